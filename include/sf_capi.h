@@ -1,0 +1,259 @@
+/*
+ * sf_capi.h -- C ABI of the GB300-native coupled SPH-DEM seepage-flow substep.
+ *
+ * One opaque handle owns the device state of one or more independent scenes
+ * (a single scene is the reference's CudaSFSystem; several scenes are the
+ * batched ensemble). Every entry point returns an sf_status, never throws and
+ * never traps; the text of the last failure is available from
+ * sf_last_error_string().
+ *
+ * Reference interfaces each entry point replaces (paths are inside the
+ * sph_seepage_flows project):
+ *   sf_create            CudaSFParticles ctor (seepage_flows_cuda/include/kiri_pbs_cuda/particle/cuda_sf_particles.cuh:131-165),
+ *                        CudaBoundaryParticles ctor (include/kiri_pbs_cuda/particle/cuda_boundary_particles.cuh:29-36),
+ *                        CudaGNSearcher / CudaGNBoundarySearcher ctors (src/kiri_pbs_cuda/searcher/cuda_neighbor_searcher.cu:19-62,118-123),
+ *                        CudaWCSphSFSolver ctor (include/kiri_pbs_cuda/solver/seepageflow/cuda_wcsph_sf_solver.cuh:22-32),
+ *                        CudaSFSystem ctor incl. boundary volume (src/kiri_pbs_cuda/system/cuda_sf_system.cu:17-64,121-136)
+ *   sf_step              CudaBaseSystem::UpdateSystem (src/kiri_pbs_cuda/system/cuda_base_system.cu:29-56)
+ *                        -> CudaSFSystem::OnUpdateSolver (src/kiri_pbs_cuda/system/cuda_sf_system.cu:66-119)
+ *   sf_num_substeps      CudaBaseSystem::GetNumOfSubTimeSteps (include/kiri_pbs_cuda/system/cuda_base_system.cuh:36)
+ *   sf_frame_adaptive    the adaptive frame loop of seepage_flows/src/seepageflow/main.cpp:235-247
+ *   sf_get_field         CudaSFParticles::Get*Ptr getters (include/kiri_pbs_cuda/particle/cuda_sf_particles.cuh:170-190)
+ *   sf_get_cell_table    CudaGNBaseSearcher::GetCellStart / GetGridSize (include/kiri_pbs_cuda/searcher/cuda_neighbor_searcher.cuh:35-44)
+ *   sf_add_sph_particles CudaSFParticles::AddSphParticles (src/kiri_pbs_cuda/particle/cuda_sf_particles.cu:50-68)
+ *   sf_run_stage         the protected per-pass methods of CudaSphSFSolver (src/kiri_pbs_cuda/solver/seepage_flow/cuda_sph_sf_solver.cu:20-402)
+ *   sf_substeps_fixed    fixed-substep mode of main.cpp:250-258 (no reference counterpart for the graph capture)
+ *   sf_create_batched    no reference counterpart (independent scenes in one launch)
+ *
+ * Threading: handles are independent; one handle must not be used from two
+ * host threads at once. All work is issued on the stream given at creation.
+ */
+#ifndef SF_CAPI_H
+#define SF_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SF_CAPI_VERSION 1
+
+typedef int32_t sf_status;
+enum {
+    SF_OK = 0,
+    SF_ERR_INVALID = 1,     /* bad argument, size or parameter */
+    SF_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    SF_ERR_CAPACITY = 3,    /* particle count would exceed the capacity */
+    SF_ERR_DEVICE = 4,      /* the device error word is set (see sf_check_error) */
+    SF_ERR_NO_DEVICE = 5,   /* no CUDA device is visible */
+    SF_ERR_UNSUPPORTED = 6  /* request not supported by this build */
+};
+
+/* CudaSphSolverType (include/kiri_pbs_cuda/data/cuda_sph_params.h:19-24) */
+enum { SF_SOLVER_SPH = 0, SF_SOLVER_WCSPH = 1 };
+/* CudaSeepageflowType (include/kiri_pbs_cuda/data/cuda_seepageflow_params.h:19-23) */
+enum { SF_TYPE_SF = 0, SF_TYPE_MULTI_SF = 1 };
+/* particle labels (include/kiri_pbs_cuda/solver/seepageflow/cuda_sph_sf_solver_gpu.cuh:434) */
+enum { SF_LABEL_WATER = 0, SF_LABEL_SAND = 1 };
+
+/* CudaSeepageflowParams (include/kiri_pbs_cuda/data/cuda_seepageflow_params.h:25-69), field for field. */
+typedef struct sf_params {
+    float sph_mass, sph_density, sph_particle_radius, sph_kernel_radius;
+    float sph_stiff, sph_visc, sph_nu, sph_bnu;
+    float dem_mass, dem_density, dem_particle_radius, dem_kernel_radius;
+    float dem_young, dem_poisson, dem_tan_friction_angle, dem_damping;
+    float sf_c0, sf_csat, sf_cmc, sf_cmc_p, sf_cd;
+    float sf_a0, sf_asat, sf_amc, sf_amc_p;
+    float sf_dry_sand_color[3];
+    float sf_wet_sand_color[3];
+    float gravity[3];
+    float dt;
+    int32_t solver_type; /* SF_SOLVER_* */
+    int32_t sf_type;     /* SF_TYPE_* */
+} sf_params;
+
+/* CudaBoundaryParams (include/kiri_pbs_cuda/data/cuda_boundary_params.h:19-27). The grid of
+ * the fluid and boundary searchers is lowest_point, kernel_radius and grid_size. */
+typedef struct sf_boundary_params {
+    float kernel_radius;
+    float lowest_point[3];
+    float highest_point[3];
+    float world_size[3];
+    float world_center[3];
+    int32_t grid_size[3];
+} sf_boundary_params;
+
+/* CudaWCSphSFSolver ctor arguments (cuda_wcsph_sf_solver.cuh:22-32) and the
+ * fixed CFL factors (cuda_wcsph_sf_solver.cuh:59-60). */
+typedef struct sf_solver_params {
+    float negative_scale;        /* default 0 */
+    float time_step_limit_scale; /* default 3 */
+    float speed_of_sound;        /* default 100 */
+} sf_solver_params;
+
+/* Host-side initial state of one scene (the vectors handed to the
+ * CudaSFParticles and CudaBoundaryParticles ctors). vel, cda0asat and amcamcp
+ * may be NULL (zero-filled, as the reference's cudaMemset-cleared arrays). */
+typedef struct sf_scene_init {
+    int64_t n;
+    const float* pos;        /* n*3 */
+    const float* vel;        /* n*3 or NULL */
+    const float* col;        /* n*3 */
+    const int32_t* label;    /* n, SF_LABEL_* */
+    const float* mass;       /* n, > 0 */
+    const float* radius;     /* n */
+    const float* cda0asat;   /* n*3 or NULL */
+    const float* amcamcp;    /* n*2 or NULL */
+    int64_t nb;
+    const float* bpos;       /* nb*3 */
+    const int32_t* blabel;   /* nb (0 = world wall, 1 = scene shape) */
+} sf_scene_init;
+
+/* Per-particle fields, named after the reference getters. */
+enum {
+    SF_FIELD_POS = 0,            /* f32 x3 */
+    SF_FIELD_VEL = 1,            /* f32 x3 */
+    SF_FIELD_ACC = 2,            /* f32 x3 */
+    SF_FIELD_COL = 3,            /* f32 x3 */
+    SF_FIELD_LABEL = 4,          /* i32 */
+    SF_FIELD_RADIUS = 5,         /* f32 */
+    SF_FIELD_MASS = 6,           /* f32 */
+    SF_FIELD_DENSITY = 7,        /* f32 */
+    SF_FIELD_PRESSURE = 8,       /* f32 */
+    SF_FIELD_VOIDAGE = 9,        /* f32 */
+    SF_FIELD_SATURATION = 10,    /* f32 */
+    SF_FIELD_MAX_SATURATION = 11,/* f32 */
+    SF_FIELD_AVG_FLOW = 12,      /* f32 x3 */
+    SF_FIELD_AVG_DRAG = 13,      /* f32 x3 (sand; 0 for water) */
+    SF_FIELD_ADHESION = 14,      /* f32 x3 (water) */
+    SF_FIELD_AVG_ADHESION = 15,  /* f32 x3 (water; 0 for sand) */
+    SF_FIELD_CDA0ASAT = 16,      /* f32 x3 */
+    SF_FIELD_AMCAMCP = 17,       /* f32 x2 */
+    SF_FIELD_ID = 18,            /* i32: creation index of the particle */
+    SF_FIELD_KEY = 19,           /* i32: scene-local cell key of the last sort */
+    SF_FIELD_COUNT = 20,
+    SF_BFIELD_POS = 32,          /* f32 x3, boundary particles in sorted order */
+    SF_BFIELD_LABEL = 33,        /* i32 */
+    SF_BFIELD_VOLUME = 34        /* f32 (Akinci volume) */
+};
+
+/* Element order of sf_get_field / sf_set_field. */
+enum {
+    SF_ORDER_SORTED = 0, /* current cell-sorted order: what the reference getters return */
+    SF_ORDER_ID = 1      /* creation order (index = particle id) */
+};
+
+/* Passes that sf_run_stage runs, in substep order. */
+enum {
+    SF_STAGE_SORT = 0,              /* hash, stable radix sort by cell, reorder, cell tables */
+    SF_STAGE_DENSITY = 1,           /* density + Tait/linear pressure */
+    SF_STAGE_AVGFLOW = 2,           /* average flow, fluid voidage, saturation */
+    SF_STAGE_VOIDAGE_ADHESION = 3,  /* sand voidage, water adhesion, wet-sand colour */
+    SF_STAGE_SAND_MOMENTUM = 4,     /* acc = g + sand forces; average drag */
+    SF_STAGE_WATER_MOMENTUM = 5,    /* acc = g + water forces; max |acc| */
+    SF_STAGE_INTEGRATE = 6,         /* CFL dt, damping, Euler, water clamp, next keys */
+    SF_STAGE_COUNT = 7
+};
+
+/* Bits of the device error word. */
+enum {
+    SF_DEVERR_NONFINITE = 1u << 0,  /* NaN/Inf in a position or acceleration */
+    SF_DEVERR_KEY_RANGE = 1u << 1,  /* a cell key outside the scene's grid */
+    SF_DEVERR_CELL_TABLE = 1u << 2, /* cell table inconsistent with the sort */
+    SF_DEVERR_TIMEOUT = 1u << 3     /* a bounded device wait gave up */
+};
+
+typedef struct sf_handle sf_handle;
+
+/* Library identification; usable without a GPU. */
+const char* sf_version(void);
+int32_t sf_capi_version(void);
+
+/* Number of visible CUDA devices (0 when none). */
+int32_t sf_device_count(void);
+
+/* Create a single-scene handle. capacity >= init->n bounds later emitter growth.
+ * stream is a cudaStream_t (NULL = the legacy default stream). */
+sf_status sf_create(const sf_params* params, const sf_boundary_params* bparams,
+                    const sf_solver_params* sparams, const sf_scene_init* init,
+                    int64_t capacity, void* stream, sf_handle** out);
+
+/* Create a handle over n_scenes independent scenes (arrays of n_scenes entries);
+ * every substep of the handle advances all scenes in the same launches. */
+sf_status sf_create_batched(int32_t n_scenes, const sf_params* params,
+                            const sf_boundary_params* bparams, const sf_solver_params* sparams,
+                            const sf_scene_init* inits, const int64_t* capacities,
+                            void* stream, sf_handle** out);
+
+sf_status sf_destroy(sf_handle* h);
+
+/* Replace the parameters of one scene (the reference reads its global params
+ * at every UpdateSystem call). */
+sf_status sf_set_params(sf_handle* h, int32_t scene, const sf_params* params);
+sf_status sf_get_params(const sf_handle* h, int32_t scene, sf_params* params);
+
+/* One reference substep of every scene: UpdateSystem(render_interval) with the
+ * CFL sub-step count (WCSPH) or render_interval/params.dt (SPH) and
+ * dt = render_interval / N_sub. n_substeps_out (scene 0's N_sub) and ms_out
+ * (elapsed device time) may be NULL. */
+sf_status sf_step(sf_handle* h, float render_interval, int64_t* n_substeps_out, float* ms_out);
+
+/* n substeps of every scene at a fixed dt, with no host synchronisation
+ * (replayed from a captured CUDA graph). */
+sf_status sf_substeps_fixed(sf_handle* h, float dt, int64_t n);
+
+/* One frame of the reference adaptive loop: while remaining > 1e-6:
+ * sf_step(remaining); remaining -= remaining / N_sub. Single-scene handles only. */
+sf_status sf_frame_adaptive(sf_handle* h, float render_interval, int64_t* n_calls_out);
+
+/* Run one pass of the substep (parity testing; the reference's per-pass
+ * solver methods). time_arg is the render interval when adaptive != 0, else dt. */
+sf_status sf_run_stage(sf_handle* h, int32_t stage, float time_arg, int32_t adaptive);
+
+/* Copy a field of one scene to dst (device pointer when dst_on_device, else
+ * host). count = number of particles (or boundary particles for SF_BFIELD_*)
+ * to copy; must equal the scene's live count. */
+sf_status sf_get_field(sf_handle* h, int32_t scene, int32_t field, int32_t order,
+                       void* dst, int64_t count, int32_t dst_on_device);
+sf_status sf_set_field(sf_handle* h, int32_t scene, int32_t field, int32_t order,
+                       const void* src, int64_t count, int32_t src_on_device);
+
+/* Cell start table of one scene (which = 0 particles, 1 boundary), as
+ * scene-relative offsets: G+1 entries, entry G = the scene's count. */
+sf_status sf_get_cell_table(sf_handle* h, int32_t scene, int32_t which, int64_t* dst, int64_t count);
+sf_status sf_get_grid(const sf_handle* h, int32_t scene, int32_t grid_size[3], int64_t* n_cells);
+
+sf_status sf_size(const sf_handle* h, int32_t scene, int64_t* n, int64_t* capacity);
+sf_status sf_num_scenes(const sf_handle* h, int32_t* n_scenes);
+sf_status sf_num_substeps(sf_handle* h, int32_t scene, int64_t* n_sub);
+
+/* Append water particles (CudaSFParticles::AddSphParticles). Returns
+ * SF_ERR_CAPACITY (and adds nothing) when size + n >= capacity, as the
+ * reference does. */
+sf_status sf_add_sph_particles(sf_handle* h, int32_t scene, const float* pos3, int64_t n,
+                               const float col[3], const float vel[3], float mass, float radius);
+
+/* Read and clear the device error word (SF_DEVERR_* bits). */
+sf_status sf_check_error(sf_handle* h, uint32_t* flags);
+
+/* Wait for all work of the handle. */
+sf_status sf_synchronize(sf_handle* h);
+
+/* Number of kernel launches the handle has issued so far (graph replays count
+ * every kernel node). */
+sf_status sf_launch_count(const sf_handle* h, int64_t* launches);
+
+/* Launch configuration of the neighbor passes: block size (multiple of 32,
+ * <= 1024) and the number of particles each thread handles; 0 keeps a value. */
+sf_status sf_set_tuning(sf_handle* h, int32_t block_size, int32_t items_per_thread);
+
+/* Text of the last error on this handle (or of the last failed create when h is NULL). */
+const char* sf_last_error_string(const sf_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SF_CAPI_H */

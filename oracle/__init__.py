@@ -1,0 +1,273 @@
+"""ORACLE -- test infrastructure, not product code.
+
+ctypes wrappers of the CPU oracle (oracle/sf_oracle.cpp -> oracle/libsforacle.so)
+and of the reference harness (oracle/ref_harness.cpp -> oracle/_ref/libsfref.so,
+built only where the reference sources are mounted). Only tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg use this package, and
+only as the checker of the CUDA path.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+from sph_seepage_flows_gb300.params import BFIELDS, FIELDS, STAGE_ID, SfBoundaryParams, SfParams, SfSceneInit, \
+    SfSolverParams
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "libsforacle.so")
+REF_SO = os.path.join(HERE, "_ref", "libsfref.so")
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle library (make -C oracle)."""
+    if force or not os.path.exists(ORACLE_SO) or \
+            os.path.getmtime(ORACLE_SO) < os.path.getmtime(os.path.join(HERE, "sf_oracle.cpp")):
+        subprocess.run(["make", "-s", "-B" if force else "-s", "-C", HERE, "libsforacle.so"], check=True)
+    return ORACLE_SO
+
+
+def build_ref() -> str | None:
+    """Compile the reference harness when the reference sources are present."""
+    subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")], check=True)
+    return REF_SO if os.path.exists(REF_SO) else None
+
+
+def _fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)) if a is not None else None
+
+
+def _iptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)) if a is not None else None
+
+
+class SceneInit:
+    """Keeps the numpy buffers of an sf_scene_init alive."""
+
+    def __init__(self, scene):
+        self.arrays = {}
+        for name in ("pos", "vel", "col", "mass", "radius", "cda0asat", "amcamcp", "bpos"):
+            self.arrays[name] = np.ascontiguousarray(getattr(scene, name), dtype=np.float32)
+        for name in ("label", "blabel"):
+            self.arrays[name] = np.ascontiguousarray(getattr(scene, name), dtype=np.int32)
+        a = self.arrays
+        self.init = SfSceneInit(n=scene.n, pos=_fptr(a["pos"]), vel=_fptr(a["vel"]), col=_fptr(a["col"]),
+                                label=_iptr(a["label"]), mass=_fptr(a["mass"]), radius=_fptr(a["radius"]),
+                                cda0asat=_fptr(a["cda0asat"]), amcamcp=_fptr(a["amcamcp"]), nb=scene.nb,
+                                bpos=_fptr(a["bpos"]), blabel=_iptr(a["blabel"]))
+
+
+def _field_meta(name):
+    if name in FIELDS:
+        return FIELDS[name]
+    if name in BFIELDS:
+        return BFIELDS[name]
+    if name == "acc_scale":
+        return (100, 1, np.float64)
+    if name == "pressure_scale":
+        return (101, 1, np.float64)
+    raise KeyError(name)
+
+
+class _Base:
+    _lib = None
+    _prefix = ""
+
+    def field(self, name: str) -> np.ndarray:
+        fid, width, _ = _field_meta(name)
+        count = self.nb if fid >= 32 and fid < 100 else self.n
+        out = np.zeros(count * width, dtype=np.float64)
+        rc = getattr(self._lib, self._prefix + "get_field")(self.h, fid, out.ctypes.data_as(
+            ctypes.POINTER(ctypes.c_double)), ctypes.c_int64(count))
+        if rc != 0:
+            raise RuntimeError(f"get_field({name}) failed: {rc}")
+        return out.reshape(count, width) if width > 1 else out
+
+    def fields(self, names=None) -> dict:
+        names = names or list(FIELDS.keys())
+        return {k: self.field(k) for k in names}
+
+    def cell_table(self, which: int = 0) -> np.ndarray:
+        g = np.asarray(self.bparams.grid_size[:], dtype=np.int64)
+        count = int(g.prod()) + 1
+        out = np.zeros(count, dtype=np.int64)
+        rc = getattr(self._lib, self._prefix + "get_cell_table")(self.h, which, out.ctypes.data_as(
+            ctypes.POINTER(ctypes.c_int64)), ctypes.c_int64(count))
+        if rc != 0:
+            raise RuntimeError("get_cell_table failed")
+        return out
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                getattr(self._lib, self._prefix + "destroy")(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+def _load_oracle():
+    build()
+    lib = ctypes.CDLL(ORACLE_SO)
+    lib.sfo_create.restype = ctypes.c_void_p
+    lib.sfo_create.argtypes = [ctypes.c_int, ctypes.POINTER(SfParams), ctypes.POINTER(SfBoundaryParams),
+                               ctypes.POINTER(SfSolverParams), ctypes.POINTER(SfSceneInit), ctypes.c_int]
+    lib.sfo_destroy.argtypes = [ctypes.c_void_p]
+    lib.sfo_get_field.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int64]
+    lib.sfo_set_field.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int64]
+    lib.sfo_get_cell_table.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int64),
+                                       ctypes.c_int64]
+    lib.sfo_run_stage.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+    lib.sfo_substeps.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int64]
+    lib.sfo_frame_adaptive.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.POINTER(ctypes.c_int64)]
+    lib.sfo_num_substeps.restype = ctypes.c_int64
+    lib.sfo_num_substeps.argtypes = [ctypes.c_void_p]
+    lib.sfo_max_acc.restype = ctypes.c_double
+    lib.sfo_max_acc.argtypes = [ctypes.c_void_p]
+    lib.sfo_set_threads.argtypes = [ctypes.c_int]
+    lib.sfo_interaction_reach.restype = ctypes.c_double
+    lib.sfo_interaction_reach.argtypes = [ctypes.POINTER(SfParams), ctypes.POINTER(SfBoundaryParams)]
+    return lib
+
+
+_ORACLE_LIB = None
+
+
+def oracle_lib():
+    global _ORACLE_LIB
+    if _ORACLE_LIB is None:
+        _ORACLE_LIB = _load_oracle()
+    return _ORACLE_LIB
+
+
+def set_threads(n: int) -> int:
+    return oracle_lib().sfo_set_threads(int(n))
+
+
+class Oracle(_Base):
+    """CPU restatement of one scene. precision 32 = reference FP32 arithmetic,
+    64 = the FP64 yardstick. sort_multi selects SearcherParticleType."""
+
+    _prefix = "sfo_"
+
+    def __init__(self, scene, precision: int = 32, sort_multi: int = 1):
+        self._lib = oracle_lib()
+        self.params, self.bparams, self.sparams = scene.params, scene.bparams, scene.sparams
+        self._init = SceneInit(scene)
+        self.n, self.nb = scene.n, scene.nb
+        self.h = self._lib.sfo_create(precision, ctypes.byref(self.params), ctypes.byref(self.bparams),
+                                      ctypes.byref(self.sparams), ctypes.byref(self._init.init), sort_multi)
+
+    def set_field(self, name: str, values) -> None:
+        fid, width, _ = _field_meta(name)
+        a = np.ascontiguousarray(np.asarray(values, dtype=np.float64).reshape(-1))
+        rc = self._lib.sfo_set_field(self.h, fid, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                     ctypes.c_int64(self.n))
+        if rc != 0:
+            raise RuntimeError(f"set_field({name}) failed")
+
+    def stage(self, name, time_arg: float = 0.0, adaptive: bool = False) -> None:
+        sid = STAGE_ID[name] if isinstance(name, str) else int(name)
+        self._lib.sfo_run_stage(self.h, sid, float(time_arg), int(adaptive))
+
+    def substeps(self, time_arg: float, adaptive: bool = False, n: int = 1) -> None:
+        self._lib.sfo_substeps(self.h, float(time_arg), int(adaptive), ctypes.c_int64(n))
+
+    def frame_adaptive(self, render_interval: float) -> int:
+        calls = ctypes.c_int64(0)
+        self._lib.sfo_frame_adaptive(self.h, float(render_interval), ctypes.byref(calls))
+        return calls.value
+
+    @property
+    def num_substeps(self) -> int:
+        return int(self._lib.sfo_num_substeps(self.h))
+
+    @property
+    def max_acc(self) -> float:
+        return float(self._lib.sfo_max_acc(self.h))
+
+
+def interaction_reach(params, bparams) -> float:
+    return float(oracle_lib().sfo_interaction_reach(ctypes.byref(params), ctypes.byref(bparams)))
+
+
+_REF_LIB = None
+
+
+def ref_lib():
+    """The reference harness library, or None where it was not built."""
+    global _REF_LIB
+    if _REF_LIB is None and os.path.exists(REF_SO):
+        lib = ctypes.CDLL(REF_SO)
+        lib.sfref_create.restype = ctypes.c_void_p
+        lib.sfref_create.argtypes = [ctypes.POINTER(SfParams), ctypes.POINTER(SfBoundaryParams),
+                                     ctypes.POINTER(SfSolverParams), ctypes.POINTER(SfSceneInit)]
+        lib.sfref_destroy.argtypes = [ctypes.c_void_p]
+        lib.sfref_substeps.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int64]
+        lib.sfref_get_field.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                        ctypes.c_int64]
+        lib.sfref_get_cell_table.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int64),
+                                             ctypes.c_int64]
+        lib.sfref_num_substeps.restype = ctypes.c_int64
+        lib.sfref_num_substeps.argtypes = [ctypes.c_void_p]
+        lib.sfref_world_boundary.restype = ctypes.c_int64
+        lib.sfref_world_boundary.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                             ctypes.c_float, ctypes.POINTER(ctypes.c_float),
+                                             ctypes.POINTER(ctypes.c_int32), ctypes.c_int64]
+        lib.sfref_emitter_points.restype = ctypes.c_int64
+        lib.sfref_emitter_points.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                             ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                             ctypes.POINTER(ctypes.c_float), ctypes.c_int64]
+        _REF_LIB = lib
+    return _REF_LIB
+
+
+class RefHarness(_Base):
+    """The reference's own kernels run on the CPU (see oracle/ref_harness.cpp)."""
+
+    _prefix = "sfref_"
+
+    def __init__(self, scene):
+        self._lib = ref_lib()
+        if self._lib is None:
+            raise RuntimeError("reference harness not built (oracle/_ref/libsfref.so)")
+        self.params, self.bparams, self.sparams = scene.params, scene.bparams, scene.sparams
+        self._init = SceneInit(scene)
+        self.n, self.nb = scene.n, scene.nb
+        self.h = self._lib.sfref_create(ctypes.byref(self.params), ctypes.byref(self.bparams),
+                                        ctypes.byref(self.sparams), ctypes.byref(self._init.init))
+
+    def substeps(self, time_arg: float, adaptive: bool = False, n: int = 1) -> None:
+        self._lib.sfref_substeps(self.h, float(time_arg), int(adaptive), ctypes.c_int64(n))
+
+    @property
+    def num_substeps(self) -> int:
+        return int(self._lib.sfref_num_substeps(self.h))
+
+
+def ref_world_boundary(lowest, highest, particle_radius):
+    lib = ref_lib()
+    lo = np.asarray(lowest, np.float32)
+    hi = np.asarray(highest, np.float32)
+    cap = 10_000_000
+    n = lib.sfref_world_boundary(_fptr(lo), _fptr(hi), float(particle_radius), None, None, 0)
+    out = np.zeros((n, 3), np.float32)
+    lab = np.zeros(n, np.int32)
+    lib.sfref_world_boundary(_fptr(lo), _fptr(hi), float(particle_radius), _fptr(out), _iptr(lab), min(n, cap))
+    return out, lab
+
+
+def ref_emitter_points(pos, vel, kind, particle_radius, r_or_w, h=0.0):
+    lib = ref_lib()
+    p = np.asarray(pos, np.float32)
+    v = np.asarray(vel, np.float32)
+    n = lib.sfref_emitter_points(_fptr(p), _fptr(v), int(kind), float(particle_radius), float(r_or_w), float(h),
+                                 None, 0)
+    out = np.zeros((n, 3), np.float32)
+    lib.sfref_emitter_points(_fptr(p), _fptr(v), int(kind), float(particle_radius), float(r_or_w), float(h),
+                             _fptr(out), n)
+    return out

@@ -1,0 +1,339 @@
+"""Seeded synthetic scenes of the benchmark workloads.
+
+The reference builds its scenes with host emitters
+(seepage_flows_cuda/src/kiri_pbs_cuda/emitter/*.cpp). Its box emitter jitters
+with an unseeded ``std::random_device`` (cuda_volume_emitter.cpp:86-99) and its
+app scene needs a bunny asset that is not distributed, so every scene here is
+generated from a seed: lattice blocks with uniform +-1% jitter per axis, the
+world-boundary shell of ``CudaBoundaryEmitter::BuildWorldBoundary``
+(cuda_boundary_emitter.cpp:12-80, restated in float32 by
+:func:`world_boundary`) and the reference parameters of main.cpp:40-83.
+
+Workloads (sizes in metres):
+
+* ``plain_small``: 8,000 sand (r = 0.01) + 32,000 water (pitch 0.02) in a
+  1 x 1 x 1 box (the 1.0 x 0.5 x 0.5 box of the spec cannot hold a 40 x 40
+  water column at 0.02 pitch; the counts are kept and the box grown).
+* ``plain_large``: ~500k sand (r = 0.005) in a trapezoidal embankment 0.4 high
+  with 1V:2H slopes + ~500k water (pitch 0.01) in a reservoir to 0.35, box
+  4.0 x 0.6 x 1.0, h = 0.02.
+* ``batched``: independent sand-block + water-column scenes with log-uniform
+  counts and per-scene friction / capillary / permeability scales.
+* ``adjoint``: 10k-sand column (32 x 32 x 10) + ~10k water at its base.
+* ``tiny``: a few thousand particles for parity fixtures.
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .params import (SF_LABEL_SAND, SF_LABEL_WATER, SF_TYPE_MULTI_SF, SfBoundaryParams, SfParams,
+                     SfSolverParams, boundary_params, reference_params, solver_params, tan_deg)
+
+WATER_COLOR = (np.array([127.0, 205.0, 255.0], dtype=np.float32) / np.float32(255.0))
+
+
+@dataclass
+class Scene:
+    name: str
+    params: SfParams
+    bparams: SfBoundaryParams
+    sparams: SfSolverParams
+    pos: np.ndarray
+    vel: np.ndarray
+    col: np.ndarray
+    label: np.ndarray
+    mass: np.ndarray
+    radius: np.ndarray
+    cda0asat: np.ndarray
+    amcamcp: np.ndarray
+    bpos: np.ndarray
+    blabel: np.ndarray
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def n(self) -> int:
+        return int(self.pos.shape[0])
+
+    @property
+    def nb(self) -> int:
+        return int(self.bpos.shape[0])
+
+    @property
+    def n_sand(self) -> int:
+        return int((self.label == SF_LABEL_SAND).sum())
+
+    @property
+    def n_water(self) -> int:
+        return int((self.label == SF_LABEL_WATER).sum())
+
+
+def world_boundary(lowest, highest, particle_radius: float):
+    """CudaBoundaryEmitter::BuildWorldBoundary (cuda_boundary_emitter.cpp:12-80)
+    in float32: six lattice planes at pitch 2r (bottom, top, back, front,
+    left, right), label 0, edges repeated as the reference repeats them."""
+    lo = np.asarray(lowest, dtype=np.float32)
+    hi = np.asarray(highest, dtype=np.float32)
+    spacing = np.float32(particle_radius) * np.float32(2.0)
+    sides = (hi - lo) / spacing
+
+    def count(s):  # for (size_t i = 0; i <= s; ++i) with the float comparison
+        return int(math.floor(float(s))) + 1 if s >= 0 else 0
+
+    def coords(base, k):
+        return (base + np.arange(k, dtype=np.float32) * spacing).astype(np.float32)
+
+    nx, ny, nz = count(sides[0]), count(sides[1]), count(sides[2])
+    X, Y, Z = coords(lo[0], nx), coords(lo[1], ny), coords(lo[2], nz)
+    planes = []
+
+    def plane(a, b, fn):
+        A, Bv = np.meshgrid(a, b, indexing="ij")
+        planes.append(fn(A.ravel(), Bv.ravel()))
+
+    full = lambda v, k: np.full(k, v, dtype=np.float32)  # noqa: E731
+    plane(X, Z, lambda a, b: np.stack([a, full(lo[1], a.size), b], 1))   # ZX bottom
+    plane(X, Z, lambda a, b: np.stack([a, full(hi[1], a.size), b], 1))   # ZX top
+    plane(X, Y, lambda a, b: np.stack([a, b, full(lo[2], a.size)], 1))   # XY back
+    plane(X, Y, lambda a, b: np.stack([a, b, full(hi[2], a.size)], 1))   # XY front
+    plane(Y, Z, lambda a, b: np.stack([full(lo[0], a.size), a, b], 1))   # YZ left
+    plane(Y, Z, lambda a, b: np.stack([full(hi[0], a.size), a, b], 1))   # YZ right
+    pos = np.concatenate(planes).astype(np.float32)
+    return pos, np.zeros(pos.shape[0], dtype=np.int32)
+
+
+def _lattice(origin, counts, pitch, rng, jitter_frac):
+    o = np.asarray(origin, dtype=np.float64)
+    idx = np.stack(np.meshgrid(*[np.arange(c) for c in counts], indexing="ij"), -1).reshape(-1, 3)
+    p = o + idx * pitch
+    if jitter_frac > 0:
+        p = p + rng.uniform(-jitter_frac * pitch, jitter_frac * pitch, size=p.shape)
+    return p.astype(np.float32)
+
+
+def _assemble(name, params, bparams, sparams, sand_pos, water_pos, sand_radius, water_radius,
+              cda0asat=None, amcamcp=None, meta=None) -> Scene:
+    ns, nw = sand_pos.shape[0], water_pos.shape[0]
+    pos = np.concatenate([sand_pos, water_pos]).astype(np.float32)
+    label = np.concatenate([np.full(ns, SF_LABEL_SAND, np.int32), np.full(nw, SF_LABEL_WATER, np.int32)])
+    sand_mass = np.float32(params.dem_density) * (np.float32(4.0) / np.float32(3.0) * np.float32(math.pi)
+                                                  * np.float32(sand_radius) ** np.float32(3))
+    mass = np.concatenate([np.full(ns, sand_mass, np.float32), np.full(nw, params.sph_mass, np.float32)])
+    radius = np.concatenate([np.full(ns, sand_radius, np.float32), np.full(nw, water_radius, np.float32)])
+    dry = np.asarray(params.sf_dry_sand_color[:], dtype=np.float32)
+    col = np.concatenate([np.tile(dry, (ns, 1)), np.tile(WATER_COLOR, (nw, 1))]).astype(np.float32)
+    if cda0asat is None:
+        cda0asat = np.array([params.sf_cd, params.sf_a0, params.sf_asat], dtype=np.float32)
+    if amcamcp is None:
+        amcamcp = np.array([params.sf_amc, params.sf_amc_p], dtype=np.float32)
+    # per-material arrays are set for sand only; water keeps the zero fill of
+    # the reference's cleared arrays (AddSphParticles never writes them)
+    cda = np.zeros((ns + nw, 3), np.float32)
+    cda[:ns] = cda0asat
+    amc = np.zeros((ns + nw, 2), np.float32)
+    amc[:ns] = amcamcp
+    lo = np.asarray(bparams.lowest_point[:], np.float32)
+    hi = np.asarray(bparams.highest_point[:], np.float32)
+    bpos, blabel = world_boundary(lo, hi, params.sph_particle_radius)
+    return Scene(name=name, params=params, bparams=bparams, sparams=sparams, pos=pos,
+                 vel=np.zeros_like(pos), col=col, label=label, mass=mass, radius=radius,
+                 cda0asat=cda, amcamcp=amc, bpos=bpos, blabel=blabel, meta=meta or {})
+
+
+def block_scene(name, box, sand_counts, water_counts, pitch, seed, sand_origin=None, water_origin=None,
+                jitter_frac=0.01, tan_phi=None, cap_scale=1.0, perm_scale=1.0, dem_density=2650.0,
+                gravity_y=-9.81) -> Scene:
+    """A sand lattice block resting on the floor at the +x end of the box and
+    a water lattice column at the -x end (the plain-small layout)."""
+    r = pitch / 2.0
+    params = reference_params(sph_radius=r, dem_radius=r, dem_density=dem_density, gravity_y=gravity_y)
+    if tan_phi is not None:
+        params.dem_tan_friction_angle = float(np.float32(tan_phi))
+    params.sf_c0 = float(np.float32(params.sf_c0 * cap_scale))
+    params.sf_cmc = float(np.float32(params.sf_cmc * cap_scale))
+    params.sf_csat = float(np.float32(params.sf_csat * cap_scale))
+    params.sf_cd = float(np.float32(params.sf_cd * perm_scale))
+    h = params.sph_kernel_radius
+    bparams = boundary_params((0.0, 0.0, 0.0), box, h)
+    sparams = solver_params()
+    rng = np.random.default_rng(seed)
+    rij = 2.0 * r  # sand radius + water radius: the DEM world-wall contact distance
+    sx, sy, sz = sand_counts
+    if sand_origin is None:
+        sand_origin = (box[0] - rij - (sx - 1) * pitch, rij, 0.5 * box[2] - 0.5 * (sz - 1) * pitch)
+    if water_origin is None:
+        water_origin = (2.0 * r, 2.0 * r, 2.0 * r)
+    sand = _lattice(sand_origin, sand_counts, pitch, rng, jitter_frac)
+    water = _lattice(water_origin, water_counts, pitch, rng, jitter_frac)
+    meta = {"seed": seed, "pitch": pitch, "box": list(box), "sand_counts": list(sand_counts),
+            "water_counts": list(water_counts), "tan_phi": params.dem_tan_friction_angle,
+            "cap_scale": cap_scale, "perm_scale": perm_scale}
+    return _assemble(name, params, bparams, sparams, sand, water, r, r, meta=meta)
+
+
+def plain_small(seed: int = 1234) -> Scene:
+    """8,000 sand spheres (20^3, r = 0.01) on the floor at x in [0.6, 1.0] and
+    a 20 x 40 x 40 water column at pitch 0.02 at x in [0, 0.4], 1 m box."""
+    return block_scene("plain_small", (1.0, 1.0, 1.0), (20, 20, 20), (20, 40, 40), 0.02, seed,
+                       sand_origin=(0.6, 0.02, 0.31), water_origin=(0.02, 0.02, 0.1))
+
+
+def tiny(seed: int = 7, sand=(10, 8, 10), water=(8, 12, 10)) -> Scene:
+    """A few-thousand-particle version of plain_small for parity fixtures:
+    a sand block and a water column that touch, in a 0.4 x 0.4 x 0.4 box."""
+    pitch = 0.02
+    return block_scene("tiny", (0.4, 0.4, 0.4), sand, water, pitch, seed,
+                       sand_origin=(0.4 - 0.02 - (sand[0] - 1) * pitch, 0.02, 0.06),
+                       water_origin=(0.4 - 0.02 - (sand[0] - 1 + water[0]) * pitch, 0.02, 0.06))
+
+
+def _embankment_points(toe, crest, height, zs, pitch, y0):
+    """Lattice points of a trapezoid (1V:2H slopes) extruded along z."""
+    base = crest + 4.0 * height
+    xs = np.arange(toe, toe + base + 1e-9, pitch)
+    ys = np.arange(y0, height + 1e-9, pitch)
+    X, Y, Z = np.meshgrid(xs, ys, zs, indexing="ij")
+    keep = (X >= toe + 2.0 * Y) & (X <= toe + base - 2.0 * Y)
+    return np.stack([X[keep], Y[keep], Z[keep]], 1)
+
+
+def _reservoir_points(x0, toe, level, zs, pitch, y0, gap):
+    xs = np.arange(x0, toe + 2.0 * level + 1e-9, pitch)
+    ys = np.arange(y0, level + 1e-9, pitch)
+    X, Y, Z = np.meshgrid(xs, ys, zs, indexing="ij")
+    keep = X < toe + 2.0 * Y - gap
+    return np.stack([X[keep], Y[keep], Z[keep]], 1)
+
+
+def plain_large(seed: int = 2024, target_sand: int = 500_000, target_water: int = 500_000) -> Scene:
+    """1M particles: sand embankment (0.4 high, 1V:2H slopes, crest solved so
+    the sand count is within 0.5% of target) and the upstream reservoir to
+    0.35 (length solved likewise) in a 4.0 x 0.6 x 1.0 box, h = 0.02."""
+    pitch, r = 0.01, 0.005
+    box = (4.0, 0.6, 1.0)
+    params = reference_params(sph_radius=r, dem_radius=r, dem_density=2650.0)
+    bparams = boundary_params((0.0, 0.0, 0.0), box, params.sph_kernel_radius)
+    rng = np.random.default_rng(seed)
+    zs_s = np.arange(2.0 * 2.0 * r, box[2] - 2.0 * r + 1e-9, pitch)     # z-min wall tests 2*rij
+    zs_w = np.arange(2.0 * r, box[2] - 2.0 * r + 1e-9, pitch)
+    y0 = 2.0 * r
+    height, level = 0.4, 0.35
+
+    def sand_for(crest, toe):
+        return _embankment_points(toe, crest, height, zs_s, pitch, y0)
+
+    # solve the reservoir length L (toe = x0 + L) for the water target
+    x0 = 2.0 * r
+
+    def water_for(L):
+        return _reservoir_points(x0, x0 + L, level, zs_w, pitch, y0, gap=pitch)
+
+    lo_L, hi_L = 0.1, 3.0
+    for _ in range(40):
+        mid = 0.5 * (lo_L + hi_L)
+        if water_for(mid).shape[0] < target_water:
+            lo_L = mid
+        else:
+            hi_L = mid
+    L = hi_L
+    toe = x0 + L
+    lo_c, hi_c = 0.0, 2.0
+    for _ in range(40):
+        mid = 0.5 * (lo_c + hi_c)
+        if sand_for(mid, toe).shape[0] < target_sand:
+            lo_c = mid
+        else:
+            hi_c = mid
+    crest = hi_c
+    sand = sand_for(crest, toe)
+    water = water_for(L)
+    sand = (sand + rng.uniform(-0.01 * pitch, 0.01 * pitch, size=sand.shape)).astype(np.float32)
+    water = (water + rng.uniform(-0.01 * pitch, 0.01 * pitch, size=water.shape)).astype(np.float32)
+    meta = {"seed": seed, "crest": crest, "reservoir_length": L, "toe": toe,
+            "n_sand": int(sand.shape[0]), "n_water": int(water.shape[0])}
+    return _assemble("plain_large", params, bparams, solver_params(), sand, water, r, r, meta=meta)
+
+
+def batched(n_scenes: int = 64, seed: int = 99, n_min: int = 2000, n_max: int = 60000):
+    """Independent scenes: counts log-uniform in [n_min, n_max], sand fraction
+    U[0.3, 0.7], friction angle U[25, 40] deg, capillary and permeability
+    scales U[0.5, 2]; each a sand block + water column in a cubic box scaled
+    to N^(1/3)."""
+    rng = np.random.default_rng(seed)
+    scenes = []
+    pitch = 0.02
+    for s in range(n_scenes):
+        n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
+        frac = rng.uniform(0.3, 0.7)
+        phi = rng.uniform(25.0, 40.0)
+        cap = rng.uniform(0.5, 2.0)
+        perm = rng.uniform(0.5, 2.0)
+        ns = max(8, int(round(n * frac)))
+        nw = max(8, n - ns)
+        side_s = max(2, int(round(ns ** (1.0 / 3.0))))
+        sand_counts = (side_s, max(2, int(round(ns / side_s / side_s))), side_s)
+        side_w = max(2, int(round((nw / 2.0) ** (1.0 / 3.0))))
+        water_counts = (side_w, max(2, int(round(nw / side_w / side_w))), side_w)
+        ext = max(sand_counts[0] + water_counts[0] + 4, sand_counts[1] + 4, water_counts[1] + 4,
+                  sand_counts[2] + 4, water_counts[2] + 4)
+        L = float(np.float32(ext * pitch + 0.04))
+        box = (L, L, L)
+        scenes.append(block_scene(f"batched_{s:02d}", box, sand_counts, water_counts, pitch,
+                                  seed * 1000 + s,
+                                  sand_origin=(L - 0.02 - (sand_counts[0] - 1) * pitch, 0.02,
+                                               0.04 + 0.5 * (L - 0.08 - (sand_counts[2] - 1) * pitch)),
+                                  water_origin=(0.02, 0.02, 0.04 + 0.5 * (L - 0.08 - (water_counts[2] - 1) * pitch)),
+                                  tan_phi=tan_deg(phi), cap_scale=cap, perm_scale=perm))
+    return scenes
+
+
+def adjoint_column(seed: int = 5) -> Scene:
+    """10,240 sand (32 x 10 x 32, r = 0.01, 0.2 m tall) with ~10k water at
+    pitch 0.02 around the column base."""
+    pitch = 0.02
+    box = (1.2, 0.6, 1.2)
+    sand_counts = (32, 10, 32)
+    water_counts = (50, 4, 50)
+    return block_scene("adjoint", box, sand_counts, water_counts, pitch, seed,
+                       sand_origin=(0.29, 0.02, 0.29), water_origin=(0.1, 0.02, 0.1))
+
+
+def remove_overlaps(scene: Scene, min_dist: float) -> Scene:
+    """Drop water particles closer than min_dist to a sand particle (used
+    where a water lattice is laid over a sand block)."""
+    sand = scene.pos[scene.label == SF_LABEL_SAND].astype(np.float64)
+    water_idx = np.nonzero(scene.label == SF_LABEL_WATER)[0]
+    if sand.size == 0 or water_idx.size == 0:
+        return scene
+    cell = min_dist
+    keys = {}
+    for k, p in enumerate(np.floor(sand / cell).astype(np.int64)):
+        keys.setdefault(tuple(p), []).append(k)
+    keep = np.ones(scene.n, dtype=bool)
+    wp = scene.pos[water_idx].astype(np.float64)
+    wc = np.floor(wp / cell).astype(np.int64)
+    for a, (p, c) in enumerate(zip(wp, wc)):
+        hit = False
+        for dx in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                for dz in (-1, 0, 1):
+                    for k in keys.get((c[0] + dx, c[1] + dy, c[2] + dz), ()):
+                        if np.sum((sand[k] - p) ** 2) < min_dist * min_dist:
+                            hit = True
+                            break
+        if hit:
+            keep[water_idx[a]] = False
+    for name in ("pos", "vel", "col", "label", "mass", "radius", "cda0asat", "amcamcp"):
+        setattr(scene, name, getattr(scene, name)[keep])
+    return scene
+
+
+WORKLOADS = {
+    "plain_small": plain_small,
+    "plain_large": plain_large,
+    "tiny": tiny,
+    "adjoint": adjoint_column,
+}
