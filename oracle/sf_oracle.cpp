@@ -853,7 +853,7 @@ struct Handle {
 };
 
 template <typename T> int getField(Sim<T>& s, int field, double* dst, int64_t count) {
-    const int64_t n = (field >= SF_BFIELD_POS) ? s.nb : s.n;
+    const int64_t n = (field >= SF_BFIELD_POS && field < 100) ? s.nb : s.n;
     if (count != n) return SF_ERR_INVALID;
     auto put3 = [&](const std::vector<V3<T>>& a) {
         for (int64_t i = 0; i < n; ++i) {

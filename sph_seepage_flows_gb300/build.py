@@ -1,0 +1,86 @@
+"""In-tree build of the CUDA library libsf_gb300.so (sm_103a) and of the C++
+drop-in facade test program.
+
+Each translation unit is compiled by nvcc in parallel into _build/, then
+linked into sph_seepage_flows_gb300/libsf_gb300.so. The library is built
+with --fmad=false and IEEE division / square root so that its FP32
+arithmetic matches the reference kernels' operation order exactly.
+"""
+
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(ROOT, "_build")
+LIB = os.path.join(PKG, "libsf_gb300.so")
+SOURCES = ["sf_kernels.cu", "sf_sort.cu", "sf_capi.cu"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    exe = os.path.join(cuda, "bin", "nvcc")
+    return exe if os.path.exists(exe) else (shutil.which("nvcc") or "nvcc")
+
+
+def common_flags() -> list:
+    return ARCH + ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-prec-div=true", "-prec-sqrt=true",
+                   "--extended-lambda", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
+                   "-I", os.path.join(ROOT, "include")]
+
+
+def _compile(src: str, extra: list) -> str:
+    obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+    cmd = [nvcc()] + common_flags() + extra + ["-c", os.path.join(CSRC, src), "-o", obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src}:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return obj
+
+
+def _stale(target: str, deps: list) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build_library(force: bool = False, verbose: bool = False, extra: list | None = None) -> str:
+    """Compile and link libsf_gb300.so; returns its path."""
+    os.makedirs(BUILD, exist_ok=True)
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "sf_capi.h")]
+    if not force and not _stale(LIB, deps):
+        return LIB
+    extra = list(extra or [])
+    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, extra), SOURCES))
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    if verbose:
+        print("built", LIB)
+    return LIB
+
+
+def ptxas_report(src: str = "sf_kernels.cu") -> str:
+    """-Xptxas -v resource usage of one translation unit (registers, spills)."""
+    os.makedirs(BUILD, exist_ok=True)
+    cmd = [nvcc()] + common_flags() + ["-Xptxas", "-v", "-c", os.path.join(CSRC, src), "-o",
+                                       os.path.join(BUILD, "ptxas_probe.o")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    return r.stdout + r.stderr
+
+
+if __name__ == "__main__":
+    if len(sys.argv) > 1 and sys.argv[1] == "ptxas":
+        print(ptxas_report(*(sys.argv[2:] or [])))
+    else:
+        print(build_library(force="-f" in sys.argv, verbose=True))

@@ -1,0 +1,253 @@
+"""ctypes binding of the C ABI (include/sf_capi.h) and a small Python host API
+over it. The CUDA library is required: every entry point raises when
+libsf_gb300.so is missing or fails to load; there is no CPU fallback.
+
+:class:`Simulation` mirrors the reference's host-side use of ``CudaSFSystem``
+(seepage_flows_cuda/src/kiri_pbs_cuda/system/cuda_sf_system.cu): construct it
+from scenes (particle and boundary vectors plus parameter structs), call
+:meth:`Simulation.step` as ``UpdateSystem``, read fields like the
+``CudaSFParticles::Get*Ptr`` getters.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import numpy as np
+
+from .params import BFIELDS, FIELDS, STAGE_ID, SfBoundaryParams, SfParams, SfSceneInit, SfSolverParams
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libsf_gb300.so")
+HEADER = os.path.join(os.path.dirname(PKG), "include", "sf_capi.h")
+
+SF_OK = 0
+STATUS = {0: "SF_OK", 1: "SF_ERR_INVALID", 2: "SF_ERR_CUDA", 3: "SF_ERR_CAPACITY", 4: "SF_ERR_DEVICE",
+          5: "SF_ERR_NO_DEVICE", 6: "SF_ERR_UNSUPPORTED"}
+ORDER = {"sorted": 0, "id": 1}
+
+_LIB = None
+
+
+class SfError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+def header_functions() -> list:
+    """Names of the functions include/sf_capi.h declares."""
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\*?\s+\*?(sf_\w+)\(", text, flags=re.M)))
+
+
+def load(path: str = LIB_PATH):
+    """Load libsf_gb300.so (built by build.build_library) and declare signatures."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(path):
+        raise OSError(f"{path} is missing: build it with sph_seepage_flows_gb300.build.build_library()")
+    lib = ctypes.CDLL(path)
+    H = ctypes.c_void_p
+    i32, i64, f32 = ctypes.c_int32, ctypes.c_int64, ctypes.c_float
+    P = ctypes.POINTER
+    sig = {
+        "sf_version": (ctypes.c_char_p, []),
+        "sf_capi_version": (i32, []),
+        "sf_device_count": (i32, []),
+        "sf_create": (i32, [P(SfParams), P(SfBoundaryParams), P(SfSolverParams), P(SfSceneInit), i64, H, P(H)]),
+        "sf_create_batched": (i32, [i32, P(SfParams), P(SfBoundaryParams), P(SfSolverParams), P(SfSceneInit),
+                                    P(i64), H, P(H)]),
+        "sf_destroy": (i32, [H]),
+        "sf_set_params": (i32, [H, i32, P(SfParams)]),
+        "sf_get_params": (i32, [H, i32, P(SfParams)]),
+        "sf_step": (i32, [H, f32, P(i64), P(f32)]),
+        "sf_substeps_fixed": (i32, [H, f32, i64]),
+        "sf_frame_adaptive": (i32, [H, f32, P(i64)]),
+        "sf_run_stage": (i32, [H, i32, f32, i32]),
+        "sf_get_field": (i32, [H, i32, i32, i32, ctypes.c_void_p, i64, i32]),
+        "sf_set_field": (i32, [H, i32, i32, i32, ctypes.c_void_p, i64, i32]),
+        "sf_get_cell_table": (i32, [H, i32, i32, P(i64), i64]),
+        "sf_get_grid": (i32, [H, i32, P(i32), P(i64)]),
+        "sf_size": (i32, [H, i32, P(i64), P(i64)]),
+        "sf_num_scenes": (i32, [H, P(i32)]),
+        "sf_num_substeps": (i32, [H, i32, P(i64)]),
+        "sf_add_sph_particles": (i32, [H, i32, P(f32), i64, P(f32), P(f32), f32, f32]),
+        "sf_check_error": (i32, [H, P(ctypes.c_uint32)]),
+        "sf_synchronize": (i32, [H]),
+        "sf_launch_count": (i32, [H, P(i64)]),
+        "sf_set_tuning": (i32, [H, i32, i32]),
+        "sf_last_error_string": (ctypes.c_char_p, [H]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def device_count() -> int:
+    return int(load().sf_device_count())
+
+
+def _fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)) if a is not None else None
+
+
+def _iptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)) if a is not None else None
+
+
+class _Init:
+    def __init__(self, scene):
+        self.keep = {}
+        for k in ("pos", "vel", "col", "mass", "radius", "cda0asat", "amcamcp", "bpos"):
+            self.keep[k] = np.ascontiguousarray(getattr(scene, k), dtype=np.float32)
+        for k in ("label", "blabel"):
+            self.keep[k] = np.ascontiguousarray(getattr(scene, k), dtype=np.int32)
+        a = self.keep
+        self.s = SfSceneInit(n=scene.n, pos=_fptr(a["pos"]), vel=_fptr(a["vel"]), col=_fptr(a["col"]),
+                             label=_iptr(a["label"]), mass=_fptr(a["mass"]), radius=_fptr(a["radius"]),
+                             cda0asat=_fptr(a["cda0asat"]), amcamcp=_fptr(a["amcamcp"]), nb=scene.nb,
+                             bpos=_fptr(a["bpos"]), blabel=_iptr(a["blabel"]))
+
+
+class Simulation:
+    """One handle over one or more scenes (a list gives the batched layout)."""
+
+    def __init__(self, scenes, capacity=None, stream=None):
+        self.lib = load()
+        single = not isinstance(scenes, (list, tuple))
+        self.scenes = [scenes] if single else list(scenes)
+        ns = len(self.scenes)
+        self._inits = [_Init(s) for s in self.scenes]
+        if capacity is None:
+            caps = [s.n for s in self.scenes]
+        elif isinstance(capacity, (list, tuple)):
+            caps = list(capacity)
+        else:
+            caps = [int(capacity)] * ns
+        self.params = (SfParams * ns)(*[s.params for s in self.scenes])
+        self.bparams = (SfBoundaryParams * ns)(*[s.bparams for s in self.scenes])
+        self.sparams = (SfSolverParams * ns)(*[s.sparams for s in self.scenes])
+        inits = (SfSceneInit * ns)(*[i.s for i in self._inits])
+        caps_arr = (ctypes.c_int64 * ns)(*caps)
+        h = ctypes.c_void_p()
+        st = self.lib.sf_create_batched(ns, self.params, self.bparams, self.sparams, inits, caps_arr,
+                                        ctypes.c_void_p(stream) if stream else None, ctypes.byref(h))
+        if st != SF_OK:
+            raise SfError(st, self.lib.sf_last_error_string(None).decode())
+        self.h = h
+
+    # ------------------------------------------------------------ helpers
+    def _check(self, st):
+        if st != SF_OK:
+            raise SfError(st, self.lib.sf_last_error_string(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def size(self, scene: int = 0) -> int:
+        n = ctypes.c_int64()
+        cap = ctypes.c_int64()
+        self._check(self.lib.sf_size(self.h, scene, ctypes.byref(n), ctypes.byref(cap)))
+        return n.value
+
+    # ------------------------------------------------------------- stepping
+    def step(self, render_interval: float, timed: bool = False):
+        """UpdateSystem(render_interval): one substep with the CFL count."""
+        nsub = ctypes.c_int64()
+        ms = ctypes.c_float()
+        self._check(self.lib.sf_step(self.h, float(render_interval), ctypes.byref(nsub),
+                                     ctypes.byref(ms) if timed else None))
+        return (nsub.value, ms.value) if timed else nsub.value
+
+    def substeps_fixed(self, dt: float, n: int):
+        self._check(self.lib.sf_substeps_fixed(self.h, float(dt), int(n)))
+
+    def frame_adaptive(self, render_interval: float) -> int:
+        calls = ctypes.c_int64()
+        self._check(self.lib.sf_frame_adaptive(self.h, float(render_interval), ctypes.byref(calls)))
+        return calls.value
+
+    def stage(self, name, time_arg: float = 0.0, adaptive: bool = False):
+        sid = STAGE_ID[name] if isinstance(name, str) else int(name)
+        self._check(self.lib.sf_run_stage(self.h, sid, float(time_arg), int(adaptive)))
+
+    def num_substeps(self, scene: int = 0) -> int:
+        v = ctypes.c_int64()
+        self._check(self.lib.sf_num_substeps(self.h, scene, ctypes.byref(v)))
+        return v.value
+
+    def synchronize(self):
+        self._check(self.lib.sf_synchronize(self.h))
+
+    def launches(self) -> int:
+        v = ctypes.c_int64()
+        self._check(self.lib.sf_launch_count(self.h, ctypes.byref(v)))
+        return v.value
+
+    def check_error(self) -> int:
+        v = ctypes.c_uint32()
+        st = self.lib.sf_check_error(self.h, ctypes.byref(v))
+        if st not in (SF_OK, 4):
+            self._check(st)
+        return v.value
+
+    def set_params(self, params: SfParams, scene: int = 0):
+        self._check(self.lib.sf_set_params(self.h, scene, ctypes.byref(params)))
+
+    # --------------------------------------------------------------- fields
+    def field(self, name: str, order: str = "sorted", scene: int = 0, out=None) -> np.ndarray:
+        """Copy a field to host memory (out: optional preallocated array)."""
+        fid, width, dt = FIELDS[name] if name in FIELDS else BFIELDS[name]
+        n = self.scenes[scene].nb if name in BFIELDS else self.size(scene)
+        shape = (n, width) if width > 1 else (n,)
+        if out is None:
+            out = np.empty(shape, dtype=dt)
+        self._check(self.lib.sf_get_field(self.h, scene, fid, ORDER[order], out.ctypes.data_as(ctypes.c_void_p),
+                                          n, 0))
+        return out
+
+    def field_device(self, name: str, dst_ptr: int, order: str = "sorted", scene: int = 0):
+        fid, _, _ = FIELDS[name]
+        self._check(self.lib.sf_get_field(self.h, scene, fid, ORDER[order], ctypes.c_void_p(dst_ptr),
+                                          self.size(scene), 1))
+
+    def set_field(self, name: str, values, order: str = "sorted", scene: int = 0):
+        fid, width, dt = FIELDS[name]
+        a = np.ascontiguousarray(values, dtype=dt)
+        self._check(self.lib.sf_set_field(self.h, scene, fid, ORDER[order], a.ctypes.data_as(ctypes.c_void_p),
+                                          self.size(scene), 0))
+
+    def fields(self, names=None, order: str = "sorted", scene: int = 0) -> dict:
+        return {k: self.field(k, order, scene) for k in (names or list(FIELDS.keys()))}
+
+    def cell_table(self, which: int = 0, scene: int = 0) -> np.ndarray:
+        g = (ctypes.c_int32 * 3)()
+        nc = ctypes.c_int64()
+        self._check(self.lib.sf_get_grid(self.h, scene, g, ctypes.byref(nc)))
+        out = np.empty(nc.value + 1, dtype=np.int64)
+        self._check(self.lib.sf_get_cell_table(self.h, scene, which,
+                                               out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), out.size))
+        return out
+
+    def add_sph_particles(self, pos, col, vel, mass: float, radius: float, scene: int = 0):
+        p = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
+        c = np.ascontiguousarray(col, dtype=np.float32)
+        v = np.ascontiguousarray(vel, dtype=np.float32)
+        self._check(self.lib.sf_add_sph_particles(self.h, scene, _fptr(p), p.shape[0], _fptr(c), _fptr(v),
+                                                  float(mass), float(radius)))
+        self.scenes[scene].meta["added"] = self.scenes[scene].meta.get("added", 0) + p.shape[0]

@@ -1,0 +1,986 @@
+// C ABI of the GB300 seepage-flow substep (include/sf_capi.h).
+//
+// A handle owns all device memory of its scenes (plain cudaMalloc; no
+// framework allocator), one CUDA stream and, for fixed-dt runs, captured
+// CUDA graphs of two substeps (the persistent arrays ping-pong between two
+// buffer sets at every sort, so two substeps return to the same buffers).
+#include "../../include/sf_capi.h"
+#include "sf_device.cuh"
+#include "sf_kernels.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+using namespace sfg;
+
+namespace {
+
+constexpr float kPiF = 3.141592653589793238462643383279502884197f;  // KIRI_PI (kiri_pbs_pch.cuh:53)
+
+thread_local std::string g_createError;
+
+struct Bez {
+    float py0, py1, px1, py2;
+};
+
+// QuadraticBezierCoeff constructor (cuda_sf_utils.cuh:40-55), host float arithmetic.
+BezierDev makeBezier(float py0, float py1, float px1, float py2) {
+    BezierDev g;
+    float a = (px1 + 1.f) / 4.f;
+    g.b = -2.f * a;
+    g.c = g.b * g.b;
+    g.d = -4.f * (1.f + g.b - px1);
+    g.e = 2.f * (1.f + g.b - px1);
+    g.py0 = py0;
+    g.py1 = py1;
+    g.px1 = px1;
+    g.py2 = py2;
+    return g;
+}
+
+// Host-side part of the scene description: every constant the reference
+// derives from the parameters alone, in the reference's float operations.
+SceneDev makeSceneDev(const sf_params& P, const sf_boundary_params& B, const sf_solver_params& Sp) {
+    SceneDev S;
+    std::memset(&S, 0, sizeof(S));
+    S.lpx = B.lowest_point[0];
+    S.lpy = B.lowest_point[1];
+    S.lpz = B.lowest_point[2];
+    S.hpx = B.highest_point[0];
+    S.hpy = B.highest_point[1];
+    S.hpz = B.highest_point[2];
+    S.cell = B.kernel_radius;
+    S.gx = B.grid_size[0];
+    S.gy = B.grid_size[1];
+    S.gz = B.grid_size[2];
+    S.ncell = S.gx * S.gy * S.gz;
+    const float h = B.kernel_radius;
+    // Poly6Kernel / SpikyKernelGrad / AdhesionAkinci13 ctors (cuda_sph_kernel.cuh:82-89,103-108,192-195)
+    S.h = h;
+    S.h2 = h * h;
+    {
+        float ih = 1.f / h;
+        float ih3 = ih * ih * ih;
+        float ih9 = ih3 * ih3 * ih3;
+        S.poly6 = 315.f * ih9 / (64.f * kPiF);
+        float h2 = h * h;
+        float h6 = h2 * h2 * h2;
+        S.spiky = -45.f / (kPiF * h6);
+        S.adh_coef = 0.007f / powf(h, 3.25f);
+        float d = S.h2 - 0.f * 0.f;
+        S.W0 = S.poly6 * d * d * d;
+    }
+    S.rho0 = P.sph_density;
+    S.rho1 = P.dem_density;
+    S.stiff = P.sph_stiff;
+    S.tait = P.solver_type == SF_SOLVER_WCSPH ? 1 : 0;
+    S.neg_scale = S.tait ? Sp.negative_scale : 1.f;
+    S.nu = P.sph_nu;
+    S.bnu = P.sph_bnu;
+    S.sph_radius = P.sph_particle_radius;
+    S.sph_mass = P.sph_mass;
+    const float r = P.dem_particle_radius;
+    S.dem_radius = r;
+    S.kn = P.dem_young * r;
+    S.ks = S.kn * P.dem_poisson;
+    S.tan2 = powf(P.dem_tan_friction_angle, 2.f);
+    S.damping = P.dem_damping;
+    S.rij2 = 2.f * r;
+    S.wall_rij = P.sph_particle_radius + r;
+    // ComputeDemCapillaryForces constants (cuda_dem_solver_common_gpu.cuh:63-65)
+    {
+        float contact_angle = 30.f / 180.f * kPiF;
+        float vlb = 4.f / 3.f * kPiF * powf(r, 3.f) * 0.01f * 0.01f;
+        float s_rupture = (1.f + 0.5f * contact_angle) * (powf(vlb, 1.f / 3.f) + 0.1f * powf(vlb, 2.f / 3.f));
+        S.cap_vlb = vlb;
+        S.cap_srupt = s_rupture;
+        S.cap_vlb_pir = vlb / (kPiF * r);
+        S.cap_pir = kPiF * r;
+        S.cap_cos = cosf(contact_angle);
+        S.cap_sin = sinf(contact_angle);
+        S.cap_m2pi = -2.f * kPiF;
+        double reach = std::max(double(h), double(2.f * r) + double(s_rupture));
+        S.reach2 = float(reach * reach * (1.0 + 1e-5));
+    }
+    S.capG = makeBezier(P.sf_c0, P.sf_cmc, P.sf_cmc_p, P.sf_csat);
+    S.multi = P.sf_type == SF_TYPE_MULTI_SF ? 1 : 0;
+    S.adhG = S.multi ? makeBezier(0.f, 1.5f, 0.5f, 0.8f) : makeBezier(P.sf_a0, P.sf_amc, P.sf_amc_p, P.sf_asat);
+    S.cd = P.sf_cd;
+    S.grav_abs = std::fabs(P.gravity[1]);
+    S.gvx = P.gravity[0];
+    S.gvy = P.gravity[1];
+    S.gvz = P.gravity[2];
+    for (int k = 0; k < 3; ++k) {
+        S.dry[k] = P.sf_dry_sand_color[k];
+        S.wet[k] = P.sf_wet_sand_color[k];
+    }
+    // ComputeSubTimeStepsByCFL (cuda_wcsph_sf_solver.cu:43-56)
+    S.cfl_by_speed = 0.4f * h / Sp.speed_of_sound;
+    S.cfl_hm = h * P.sph_mass;
+    S.cfl_mass = P.sph_mass;
+    S.cfl_scale = Sp.time_step_limit_scale;
+    S.params_dt = P.dt;
+    S.wcsph = S.tait;
+    return S;
+}
+
+// Pos2GridHash on the host (helper_thrust.cuh:66-89), same float arithmetic.
+int hostHash(const SceneDev& S, float x, float y, float z) {
+    auto axis = [](float rel, float cell, int g) {
+        float q = rel / cell;
+        int v;
+        if (!(q == q)) v = 0;
+        else if (q >= 2147483520.f) v = 2147483647;
+        else if (q <= -2147483648.f) v = INT32_MIN;
+        else v = int(q);
+        return std::min(std::max(v, 0), g - 1);
+    };
+    int cx = axis(x - S.lpx, S.cell, S.gx), cy = axis(y - S.lpy, S.cell, S.gy), cz = axis(z - S.lpz, S.cell, S.gz);
+    return cx * S.gy * S.gz + cy * S.gz + cz;
+}
+
+template <typename T> void devFree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+struct GraphCache {
+    cudaGraphExec_t exec = nullptr;
+    float dt = 0.f;
+    int nodes = 0;
+};
+
+}  // namespace
+
+struct sf_handle {
+    cudaStream_t stream = nullptr;
+    bool ownStream = false;
+    int device = 0;
+    int nScenes = 0;
+    std::vector<sf_params> P;
+    std::vector<sf_boundary_params> B;
+    std::vector<sf_solver_params> Sp;
+    std::vector<SceneDev> hScenes;
+    std::vector<int64_t> n, capUser, nextId;
+    int totalSlots = 0, totalCells = 0, totalB = 0, sortBits = 1, slotBlocks = 0;
+    SceneDev* dScenes = nullptr;
+    int* dBlockScene = nullptr;
+    SceneState* dState = nullptr;
+    unsigned int* dErr = nullptr;
+    // persistent per-slot arrays, two buffer sets
+    float4* pos[2] = {nullptr, nullptr};
+    float4* vel[2] = {nullptr, nullptr};
+    float4* col[2] = {nullptr, nullptr};
+    float4* mat[2] = {nullptr, nullptr};
+    float2* amc[2] = {nullptr, nullptr};
+    int* pid[2] = {nullptr, nullptr};
+    int cur = 0;
+    // per-substep arrays
+    float4 *aux = nullptr, *flow = nullptr, *adh = nullptr, *avgadh = nullptr, *drag = nullptr, *acc = nullptr;
+    unsigned int *keys = nullptr, *cs = nullptr, *bcs = nullptr;
+    unsigned int* sortedKeys = nullptr;  // points into keys/scratch after a sort
+    SortScratch sc{};
+    float4* bpos = nullptr;
+    int* blabel = nullptr;
+    // staging for field access
+    void* stage = nullptr;
+    size_t stageBytes = 0;
+    bool sorted = false;
+    int64_t launches = 0;
+    GraphCache graph[2];
+    std::string err;
+
+    sf_status fail(sf_status st, const std::string& msg) {
+        err = msg;
+        return st;
+    }
+    sf_status cuda(cudaError_t e, const char* what) {
+        if (e == cudaSuccess) return SF_OK;
+        err = std::string(what) + ": " + cudaGetErrorString(e);
+        return SF_ERR_CUDA;
+    }
+    LaunchCtx ctx() const {
+        LaunchCtx c;
+        c.stream = stream;
+        c.scenes = dScenes;
+        c.blockScene = dBlockScene;
+        c.state = dState;
+        c.errWord = dErr;
+        c.slotBlocks = slotBlocks;
+        return c;
+    }
+    PassBuffers buffers() const {
+        PassBuffers b;
+        b.cs = cs;
+        b.bcs = bcs;
+        b.pos4 = pos[cur];
+        b.vel4 = vel[cur];
+        b.aux4 = aux;
+        b.flow4 = flow;
+        b.adh4 = adh;
+        b.avgadh4 = avgadh;
+        b.drag4 = drag;
+        b.acc4 = acc;
+        b.col4 = col[cur];
+        b.mat4 = mat[cur];
+        b.bpos4 = bpos;
+        return b;
+    }
+    ~sf_handle() {
+        for (auto& g : graph)
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+        for (int k = 0; k < 2; ++k) {
+            devFree(pos[k]);
+            devFree(vel[k]);
+            devFree(col[k]);
+            devFree(mat[k]);
+            devFree(amc[k]);
+            devFree(pid[k]);
+        }
+        devFree(aux);
+        devFree(flow);
+        devFree(adh);
+        devFree(avgadh);
+        devFree(drag);
+        devFree(acc);
+        devFree(keys);
+        devFree(cs);
+        devFree(bcs);
+        devFree(sc.keysAlt);
+        devFree(sc.vals);
+        devFree(sc.valsAlt);
+        devFree(sc.hist);
+        devFree(bpos);
+        devFree(blabel);
+        devFree(dScenes);
+        devFree(dBlockScene);
+        devFree(dState);
+        devFree(dErr);
+        if (stage) cudaFree(stage);
+        if (ownStream && stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+// The sort stage: keys, stable radix sort, cell table, reorder into the other buffer set.
+sf_status runSort(sf_handle* h) {
+    LaunchCtx c = h->ctx();
+    launchKeys(c, h->pos[h->cur], h->keys);
+    unsigned int* perm = nullptr;
+    int l = radixSort(h->stream, h->totalSlots, h->sortBits, h->keys, h->sc, &h->sortedKeys, &perm);
+    launchCellStart(h->stream, h->totalSlots, h->totalCells, h->sortedKeys, h->cs);
+    const int o = h->cur, t = 1 - h->cur;
+    launchReorder(h->stream, h->totalSlots, perm, h->pos[o], h->vel[o], h->col[o], h->mat[o], h->amc[o], h->pid[o],
+                  h->pos[t], h->vel[t], h->col[t], h->mat[t], h->amc[t], h->pid[t]);
+    h->cur = t;
+    h->sorted = true;
+    h->launches += 3 + l;
+    return h->cuda(cudaGetLastError(), "sort stage launch");
+}
+
+sf_status runStage(sf_handle* h, int stage, float timeArg, int adaptive) {
+    LaunchCtx c = h->ctx();
+    PassBuffers b = h->buffers();
+    switch (stage) {
+    case SF_STAGE_SORT: return runSort(h);
+    case SF_STAGE_DENSITY: launchDensity(c, b); break;
+    case SF_STAGE_AVGFLOW: launchAvgFlow(c, b); break;
+    case SF_STAGE_VOIDAGE_ADHESION: launchVoidageAdhesion(c, b); break;
+    case SF_STAGE_SAND_MOMENTUM: launchSandMomentum(c, b); break;
+    case SF_STAGE_WATER_MOMENTUM: launchWaterMomentum(c, b); break;
+    case SF_STAGE_INTEGRATE: launchIntegrate(c, b, timeArg, adaptive); break;
+    default: return h->fail(SF_ERR_INVALID, "unknown stage");
+    }
+    h->launches += 1;
+    return h->cuda(cudaGetLastError(), "stage launch");
+}
+
+sf_status runSubstep(sf_handle* h, float timeArg, int adaptive) {
+    for (int s = 0; s < SF_STAGE_COUNT; ++s) {
+        sf_status st = runStage(h, s, timeArg, adaptive);
+        if (st != SF_OK) return st;
+    }
+    return SF_OK;
+}
+
+bool validScene(const sf_params* p, const sf_boundary_params* b, const sf_scene_init* in, int64_t cap,
+                std::string& why) {
+    if (!p || !b || !in) return why = "null params or init", false;
+    if (in->n < 0 || in->nb < 0) return why = "negative particle count", false;
+    if (cap < in->n) return why = "capacity smaller than the particle count", false;
+    if (cap > (int64_t(1) << 30)) return why = "capacity above 2^30 slots", false;
+    if (in->n > 0 && (!in->pos || !in->col || !in->label || !in->mass || !in->radius))
+        return why = "missing per-particle input array", false;
+    if (in->nb > 0 && !in->bpos) return why = "missing boundary positions", false;
+    if (!(b->kernel_radius > 0.f)) return why = "kernel_radius must be > 0", false;
+    for (int k = 0; k < 3; ++k)
+        if (b->grid_size[k] <= 0) return why = "grid_size must be positive", false;
+    if (int64_t(b->grid_size[0]) * b->grid_size[1] * b->grid_size[2] > (int64_t(1) << 30))
+        return why = "grid above 2^30 cells", false;
+    if (p->solver_type != SF_SOLVER_SPH && p->solver_type != SF_SOLVER_WCSPH) return why = "bad solver_type", false;
+    if (p->sf_type != SF_TYPE_SF && p->sf_type != SF_TYPE_MULTI_SF) return why = "bad sf_type", false;
+    for (int64_t i = 0; i < in->n; ++i) {
+        if (in->label[i] != SF_LABEL_WATER && in->label[i] != SF_LABEL_SAND)
+            return why = "labels must be 0 (water) or 1 (sand)", false;
+        if (!(in->mass[i] > 0.f) || !std::isfinite(in->mass[i])) return why = "masses must be finite and > 0", false;
+    }
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* sf_version(void) { return "sph_seepage_flows_gb300 0.1.0 (sm_103a)"; }
+int32_t sf_capi_version(void) { return SF_CAPI_VERSION; }
+
+int32_t sf_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+sf_status sf_create(const sf_params* params, const sf_boundary_params* bparams, const sf_solver_params* sparams,
+                    const sf_scene_init* init, int64_t capacity, void* stream, sf_handle** out) {
+    return sf_create_batched(1, params, bparams, sparams, init, &capacity, stream, out);
+}
+
+sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_boundary_params* bparams,
+                            const sf_solver_params* sparams, const sf_scene_init* inits, const int64_t* capacities,
+                            void* stream, sf_handle** out) {
+    if (!out) return SF_ERR_INVALID;
+    *out = nullptr;
+    if (n_scenes <= 0 || !params || !bparams || !sparams || !inits || !capacities) {
+        g_createError = "invalid arguments";
+        return SF_ERR_INVALID;
+    }
+    for (int s = 0; s < n_scenes; ++s) {
+        std::string why;
+        if (!validScene(&params[s], &bparams[s], &inits[s], capacities[s], why)) {
+            g_createError = "scene " + std::to_string(s) + ": " + why;
+            return SF_ERR_INVALID;
+        }
+    }
+    if (sf_device_count() <= 0) {
+        g_createError = "no CUDA device visible";
+        return SF_ERR_NO_DEVICE;
+    }
+    sf_handle* h = new (std::nothrow) sf_handle();
+    if (!h) return SF_ERR_INVALID;
+    auto bail = [&](sf_status st) {
+        g_createError = h->err;
+        delete h;
+        return st;
+    };
+    cudaGetDevice(&h->device);
+    if (stream) {
+        h->stream = static_cast<cudaStream_t>(stream);
+    } else {
+        if (h->cuda(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "cudaStreamCreate"))
+            return bail(SF_ERR_CUDA);
+        h->ownStream = true;
+    }
+    h->nScenes = n_scenes;
+    h->P.assign(params, params + n_scenes);
+    h->B.assign(bparams, bparams + n_scenes);
+    h->Sp.assign(sparams, sparams + n_scenes);
+    h->n.resize(n_scenes);
+    h->capUser.resize(n_scenes);
+    h->nextId.resize(n_scenes);
+    std::vector<int> blockScene;
+    int slotOff = 0, cellOff = 0, bOff = 0;
+    for (int s = 0; s < n_scenes; ++s) {
+        SceneDev S = makeSceneDev(params[s], bparams[s], sparams[s]);
+        const int64_t cap = std::max<int64_t>(capacities[s], 1);
+        const int slots = int((cap + kSlotAlign - 1) / kSlotAlign) * kSlotAlign;
+        S.slot_off = slotOff;
+        S.slot_cap = slots;
+        S.cell_off = cellOff;
+        S.b_off = bOff;
+        S.nb = int(inits[s].nb);
+        h->hScenes.push_back(S);
+        for (int k = 0; k < slots / kSlotAlign; ++k) blockScene.push_back(s);
+        slotOff += slots;
+        cellOff += S.ncell + 1;
+        bOff += S.nb;
+        h->n[s] = inits[s].n;
+        h->capUser[s] = capacities[s];
+        h->nextId[s] = inits[s].n;
+    }
+    h->totalSlots = slotOff;
+    h->totalCells = cellOff;
+    h->totalB = bOff;
+    h->slotBlocks = slotOff / kSlotAlign;
+    h->sortBits = 1;
+    while ((int64_t(1) << h->sortBits) <= int64_t(h->totalCells)) ++h->sortBits;
+    const size_t M = size_t(h->totalSlots);
+    const size_t F4 = sizeof(float4) * M;
+#define SF_ALLOC(ptr, bytes)                                                             \
+    if (h->cuda(cudaMalloc(reinterpret_cast<void**>(&(ptr)), (bytes)), "cudaMalloc " #ptr)) \
+        return bail(SF_ERR_CUDA);                                                        \
+    if (h->cuda(cudaMemsetAsync((ptr), 0, (bytes), h->stream), "cudaMemset " #ptr)) return bail(SF_ERR_CUDA);
+    for (int k = 0; k < 2; ++k) {
+        SF_ALLOC(h->pos[k], F4);
+        SF_ALLOC(h->vel[k], F4);
+        SF_ALLOC(h->col[k], F4);
+        SF_ALLOC(h->mat[k], F4);
+        SF_ALLOC(h->amc[k], sizeof(float2) * M);
+        SF_ALLOC(h->pid[k], sizeof(int) * M);
+    }
+    SF_ALLOC(h->aux, F4);
+    SF_ALLOC(h->flow, F4);
+    SF_ALLOC(h->adh, F4);
+    SF_ALLOC(h->avgadh, F4);
+    SF_ALLOC(h->drag, F4);
+    SF_ALLOC(h->acc, F4);
+    SF_ALLOC(h->keys, sizeof(unsigned) * M);
+    SF_ALLOC(h->sc.keysAlt, sizeof(unsigned) * M);
+    SF_ALLOC(h->sc.vals, sizeof(unsigned) * M);
+    SF_ALLOC(h->sc.valsAlt, sizeof(unsigned) * M);
+    h->sc.tiles = sortTiles(h->totalSlots);
+    SF_ALLOC(h->sc.hist, sizeof(unsigned) * 256 * size_t(h->sc.tiles));
+    SF_ALLOC(h->cs, sizeof(unsigned) * (size_t(h->totalCells) + 1));
+    SF_ALLOC(h->bcs, sizeof(unsigned) * (size_t(h->totalCells) + 1));
+    SF_ALLOC(h->bpos, sizeof(float4) * std::max<size_t>(1, size_t(h->totalB)));
+    SF_ALLOC(h->blabel, sizeof(int) * std::max<size_t>(1, size_t(h->totalB)));
+    SF_ALLOC(h->dScenes, sizeof(SceneDev) * n_scenes);
+    SF_ALLOC(h->dBlockScene, sizeof(int) * blockScene.size());
+    SF_ALLOC(h->dState, sizeof(SceneState) * n_scenes);
+    SF_ALLOC(h->dErr, sizeof(unsigned));
+#undef SF_ALLOC
+    // host staging of the initial state
+    std::vector<float4> hpos(M, make_float4(0, 0, 0, 0)), hvel(M, make_float4(0, 0, 0, 0)),
+        hcol(M, make_float4(0, 0, 0, 0)), hmat(M, make_float4(0, 0, 0, 0));
+    std::vector<float2> hamc(M, make_float2(0, 0));
+    std::vector<int> hpid(M, -1);
+    std::vector<float4> hbpos(std::max(1, h->totalB), make_float4(0, 0, 0, 0));
+    std::vector<int> hblabel(std::max(1, h->totalB), 0);
+    std::vector<unsigned> hbcs(size_t(h->totalCells) + 1, 0);
+    std::vector<SceneState> hstate(n_scenes);
+    for (int s = 0; s < n_scenes; ++s) {
+        const sf_scene_init& in = inits[s];
+        const SceneDev& S = h->hScenes[s];
+        for (int64_t i = 0; i < in.n; ++i) {
+            const size_t k = size_t(S.slot_off + i);
+            const float m = in.mass[i];
+            hpos[k] = make_float4(in.pos[3 * i], in.pos[3 * i + 1], in.pos[3 * i + 2],
+                                  in.label[i] == SF_LABEL_SAND ? -m : m);
+            if (in.vel) hvel[k] = make_float4(in.vel[3 * i], in.vel[3 * i + 1], in.vel[3 * i + 2], 0.f);
+            hcol[k] = make_float4(in.col[3 * i], in.col[3 * i + 1], in.col[3 * i + 2], 0.f);
+            float4 mt = make_float4(0.f, 0.f, 0.f, in.radius[i]);
+            if (in.cda0asat) {
+                mt.x = in.cda0asat[3 * i];
+                mt.y = in.cda0asat[3 * i + 1];
+                mt.z = in.cda0asat[3 * i + 2];
+            }
+            hmat[k] = mt;
+            if (in.amcamcp) hamc[k] = make_float2(in.amcamcp[2 * i], in.amcamcp[2 * i + 1]);
+            hpid[k] = int(i);
+        }
+        // boundary searcher: stable sort by cell + cell table (cuda_neighbor_searcher.cu:36-51,125-139)
+        std::vector<int> bk(static_cast<size_t>(in.nb));
+        for (int64_t i = 0; i < in.nb; ++i) bk[i] = hostHash(S, in.bpos[3 * i], in.bpos[3 * i + 1], in.bpos[3 * i + 2]);
+        std::vector<int64_t> order(static_cast<size_t>(in.nb));
+        for (int64_t i = 0; i < in.nb; ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return bk[a] < bk[b]; });
+        std::vector<unsigned> cnt(static_cast<size_t>(S.ncell) + 1, 0u);
+        for (int64_t i = 0; i < in.nb; ++i) cnt[bk[i]]++;
+        unsigned run = unsigned(S.b_off);
+        for (int c = 0; c <= S.ncell; ++c) {
+            hbcs[size_t(S.cell_off + c)] = run;
+            run += cnt[c];
+        }
+        for (int64_t i = 0; i < in.nb; ++i) {
+            const int64_t o = order[i];
+            hbpos[size_t(S.b_off + i)] = make_float4(in.bpos[3 * o], in.bpos[3 * o + 1], in.bpos[3 * o + 2], 0.f);
+            hblabel[size_t(S.b_off + i)] = in.blabel ? in.blabel[o] : 0;
+        }
+        hstate[s].n = int(in.n);
+        hstate[s].n_sub = 1;
+    }
+    hbcs[size_t(h->totalCells)] = unsigned(h->totalB);
+    auto up = [&](void* d, const void* src, size_t bytes, const char* what) {
+        return h->cuda(cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, h->stream), what);
+    };
+    if (up(h->pos[0], hpos.data(), F4, "upload pos") || up(h->vel[0], hvel.data(), F4, "upload vel") ||
+        up(h->col[0], hcol.data(), F4, "upload col") || up(h->mat[0], hmat.data(), F4, "upload mat") ||
+        up(h->amc[0], hamc.data(), sizeof(float2) * M, "upload amc") ||
+        up(h->pid[0], hpid.data(), sizeof(int) * M, "upload pid") ||
+        up(h->bpos, hbpos.data(), sizeof(float4) * hbpos.size(), "upload bpos") ||
+        up(h->blabel, hblabel.data(), sizeof(int) * hblabel.size(), "upload blabel") ||
+        up(h->bcs, hbcs.data(), sizeof(unsigned) * hbcs.size(), "upload bcs") ||
+        up(h->dScenes, h->hScenes.data(), sizeof(SceneDev) * n_scenes, "upload scenes") ||
+        up(h->dBlockScene, blockScene.data(), sizeof(int) * blockScene.size(), "upload blockScene") ||
+        up(h->dState, hstate.data(), sizeof(SceneState) * n_scenes, "upload state"))
+        return bail(SF_ERR_CUDA);
+    // Akinci boundary volume (cuda_sf_system.cu:121-136)
+    LaunchCtx c = h->ctx();
+    for (int s = 0; s < n_scenes; ++s) {
+        launchBoundaryVolume(c, s, h->hScenes[s].nb, h->bpos, h->blabel, h->bcs);
+        h->launches += h->hScenes[s].nb > 0 ? 1 : 0;
+    }
+    if (h->cuda(cudaGetLastError(), "boundary volume") || h->cuda(cudaStreamSynchronize(h->stream), "create sync"))
+        return bail(SF_ERR_CUDA);
+    *out = h;
+    return SF_OK;
+}
+
+sf_status sf_destroy(sf_handle* h) {
+    if (!h) return SF_ERR_INVALID;
+    cudaStreamSynchronize(h->stream);
+    delete h;
+    return SF_OK;
+}
+
+sf_status sf_set_params(sf_handle* h, int32_t scene, const sf_params* p) {
+    if (!h || !p || scene < 0 || scene >= h->nScenes) return SF_ERR_INVALID;
+    if (p->solver_type != SF_SOLVER_SPH && p->solver_type != SF_SOLVER_WCSPH)
+        return h->fail(SF_ERR_INVALID, "bad solver_type");
+    if (p->sf_type != SF_TYPE_SF && p->sf_type != SF_TYPE_MULTI_SF) return h->fail(SF_ERR_INVALID, "bad sf_type");
+    h->P[scene] = *p;
+    SceneDev S = makeSceneDev(*p, h->B[scene], h->Sp[scene]);
+    const SceneDev& old = h->hScenes[scene];
+    S.slot_off = old.slot_off;
+    S.slot_cap = old.slot_cap;
+    S.cell_off = old.cell_off;
+    S.b_off = old.b_off;
+    S.nb = old.nb;
+    h->hScenes[scene] = S;
+    return h->cuda(cudaMemcpyAsync(h->dScenes + scene, &S, sizeof(SceneDev), cudaMemcpyHostToDevice, h->stream),
+                   "upload params");
+}
+
+sf_status sf_get_params(const sf_handle* h, int32_t scene, sf_params* p) {
+    if (!h || !p || scene < 0 || scene >= h->nScenes) return SF_ERR_INVALID;
+    *p = h->P[scene];
+    return SF_OK;
+}
+
+sf_status sf_run_stage(sf_handle* h, int32_t stage, float time_arg, int32_t adaptive) {
+    if (!h) return SF_ERR_INVALID;
+    if (stage < 0 || stage >= SF_STAGE_COUNT) return h->fail(SF_ERR_INVALID, "unknown stage");
+    if (stage != SF_STAGE_SORT && !h->sorted) return h->fail(SF_ERR_INVALID, "run the sort stage first");
+    return runStage(h, stage, time_arg, adaptive);
+}
+
+sf_status sf_step(sf_handle* h, float render_interval, int64_t* n_substeps_out, float* ms_out) {
+    if (!h) return SF_ERR_INVALID;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (ms_out) {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, h->stream);
+    }
+    sf_status st = runSubstep(h, render_interval, 1);
+    if (st != SF_OK) return st;
+    if (ms_out) {
+        cudaEventRecord(e1, h->stream);
+        cudaEventSynchronize(e1);
+        cudaEventElapsedTime(ms_out, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    if (n_substeps_out) {
+        SceneState s0;
+        st = h->cuda(cudaMemcpyAsync(&s0, h->dState, sizeof(SceneState), cudaMemcpyDeviceToHost, h->stream),
+                     "read n_sub");
+        if (st) return st;
+        st = h->cuda(cudaStreamSynchronize(h->stream), "sync");
+        if (st) return st;
+        *n_substeps_out = s0.n_sub;
+    }
+    return h->cuda(cudaGetLastError(), "sf_step");
+}
+
+sf_status sf_frame_adaptive(sf_handle* h, float render_interval, int64_t* n_calls_out) {
+    if (!h) return SF_ERR_INVALID;
+    if (h->nScenes != 1) return h->fail(SF_ERR_UNSUPPORTED, "sf_frame_adaptive needs a single-scene handle");
+    float remaining = render_interval;
+    int64_t calls = 0;
+    while (remaining > kEps) {  // main.cpp:240-247
+        int64_t nsub = 0;
+        sf_status st = sf_step(h, remaining, &nsub, nullptr);
+        if (st != SF_OK) return st;
+        if (nsub <= 0) return h->fail(SF_ERR_INVALID, "CFL gave zero sub-steps for the remaining time");
+        remaining -= remaining / float(nsub);
+        ++calls;
+    }
+    if (n_calls_out) *n_calls_out = calls;
+    return SF_OK;
+}
+
+sf_status sf_substeps_fixed(sf_handle* h, float dt, int64_t n) {
+    if (!h || n < 0) return SF_ERR_INVALID;
+    int64_t k = 0;
+    // odd remainder (or a single step) without a graph
+    if (n % 2 == 1) {
+        sf_status st = runSubstep(h, dt, 0);
+        if (st != SF_OK) return st;
+        k = 1;
+    }
+    if (n - k <= 0) return SF_OK;
+    GraphCache& g = h->graph[h->cur];
+    if (!g.exec || g.dt != dt) {
+        if (g.exec) {
+            cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+        }
+        const int curBefore = h->cur;
+        const int64_t launchesBefore = h->launches;
+        cudaGraph_t graph = nullptr;
+        sf_status st = h->cuda(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        if (st) return st;
+        sf_status s1 = runSubstep(h, dt, 0);
+        sf_status s2 = s1 == SF_OK ? runSubstep(h, dt, 0) : s1;
+        cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+        h->cur = curBefore;
+        g.nodes = int(h->launches - launchesBefore);
+        h->launches = launchesBefore;
+        if (s2 != SF_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return s2;
+        }
+        if (h->cuda(ce, "end capture")) return SF_ERR_CUDA;
+        st = h->cuda(cudaGraphInstantiate(&g.exec, graph, 0), "graph instantiate");
+        cudaGraphDestroy(graph);
+        if (st) return st;
+        g.dt = dt;
+    }
+    for (; k + 2 <= n; k += 2) {
+        sf_status st = h->cuda(cudaGraphLaunch(g.exec, h->stream), "graph launch");
+        if (st) return st;
+        h->launches += g.nodes;
+    }
+    h->sorted = true;
+    return SF_OK;
+}
+
+// ---------------------------------------------------------------- fields
+namespace {
+
+__global__ void kGetField(int field, int n, int slotOff, int cellOff, int order, const float4* __restrict__ pos,
+                          const float4* __restrict__ vel, const float4* __restrict__ col,
+                          const float4* __restrict__ mat, const float2* __restrict__ amc,
+                          const int* __restrict__ pid, const float4* __restrict__ aux, const float4* __restrict__ flow,
+                          const float4* __restrict__ adh, const float4* __restrict__ avgadh,
+                          const float4* __restrict__ drag, const float4* __restrict__ acc,
+                          const unsigned int* __restrict__ keys, void* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int s = slotOff + i;
+    const int o = order == SF_ORDER_ID ? pid[s] : i;
+    float* f = static_cast<float*>(out);
+    int* iv = static_cast<int*>(out);
+    auto put3 = [&](float4 v) {
+        f[3 * o] = v.x;
+        f[3 * o + 1] = v.y;
+        f[3 * o + 2] = v.z;
+    };
+    switch (field) {
+    case SF_FIELD_POS: put3(pos[s]); break;
+    case SF_FIELD_VEL: put3(vel[s]); break;
+    case SF_FIELD_ACC: put3(acc[s]); break;
+    case SF_FIELD_COL: put3(col[s]); break;
+    case SF_FIELD_LABEL: iv[o] = pos[s].w < 0.f ? SF_LABEL_SAND : SF_LABEL_WATER; break;
+    case SF_FIELD_RADIUS: f[o] = mat[s].w; break;
+    case SF_FIELD_MASS: f[o] = fabsf(pos[s].w); break;
+    case SF_FIELD_DENSITY: f[o] = vel[s].w; break;
+    case SF_FIELD_PRESSURE: f[o] = aux[s].x; break;
+    case SF_FIELD_VOIDAGE: f[o] = aux[s].w; break;
+    case SF_FIELD_SATURATION: f[o] = aux[s].z; break;
+    case SF_FIELD_MAX_SATURATION: f[o] = col[s].w; break;
+    case SF_FIELD_AVG_FLOW: put3(flow[s]); break;
+    case SF_FIELD_AVG_DRAG: put3(drag[s]); break;
+    case SF_FIELD_ADHESION: put3(adh[s]); break;
+    case SF_FIELD_AVG_ADHESION: put3(avgadh[s]); break;
+    case SF_FIELD_CDA0ASAT: put3(mat[s]); break;
+    case SF_FIELD_AMCAMCP:
+        f[2 * o] = amc[s].x;
+        f[2 * o + 1] = amc[s].y;
+        break;
+    case SF_FIELD_ID: iv[o] = pid[s]; break;
+    case SF_FIELD_KEY: iv[o] = keys ? int(keys[s]) - cellOff : -1; break;
+    default: break;
+    }
+}
+
+__global__ void kSetField(int field, int n, int slotOff, int order, float4* pos, float4* vel, float4* col,
+                          float4* mat, float2* amc, const int* __restrict__ pid, float4* aux, float4* flow,
+                          float4* adh, float4* avgadh, float4* drag, float4* acc, const void* in) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int s = slotOff + i;
+    const int o = order == SF_ORDER_ID ? pid[s] : i;
+    const float* f = static_cast<const float*>(in);
+    const int* iv = static_cast<const int*>(in);
+    auto set3 = [&](float4* a) {
+        float4 v = a[s];
+        v.x = f[3 * o];
+        v.y = f[3 * o + 1];
+        v.z = f[3 * o + 2];
+        a[s] = v;
+    };
+    switch (field) {
+    case SF_FIELD_POS: set3(pos); break;
+    case SF_FIELD_VEL: set3(vel); break;
+    case SF_FIELD_ACC: set3(acc); break;
+    case SF_FIELD_COL: set3(col); break;
+    case SF_FIELD_LABEL: {
+        const float m = fabsf(pos[s].w);
+        pos[s].w = iv[o] == SF_LABEL_SAND ? -m : m;
+        break;
+    }
+    case SF_FIELD_RADIUS: mat[s].w = f[o]; break;
+    case SF_FIELD_MASS: pos[s].w = pos[s].w < 0.f ? -f[o] : f[o]; break;
+    case SF_FIELD_DENSITY: vel[s].w = f[o]; break;
+    case SF_FIELD_PRESSURE: aux[s].x = f[o]; break;
+    case SF_FIELD_VOIDAGE: aux[s].w = f[o]; aux[s].y = f[o]; break;
+    case SF_FIELD_SATURATION: aux[s].z = f[o]; break;
+    case SF_FIELD_MAX_SATURATION: col[s].w = f[o]; break;
+    case SF_FIELD_AVG_FLOW: set3(flow); break;
+    case SF_FIELD_AVG_DRAG: set3(drag); break;
+    case SF_FIELD_ADHESION: set3(adh); break;
+    case SF_FIELD_AVG_ADHESION: set3(avgadh); break;
+    case SF_FIELD_CDA0ASAT: set3(mat); break;
+    case SF_FIELD_AMCAMCP: amc[s] = make_float2(f[2 * o], f[2 * o + 1]); break;
+    default: break;
+    }
+}
+
+int fieldWidth(int field) {
+    switch (field) {
+    case SF_FIELD_POS: case SF_FIELD_VEL: case SF_FIELD_ACC: case SF_FIELD_COL: case SF_FIELD_AVG_FLOW:
+    case SF_FIELD_AVG_DRAG: case SF_FIELD_ADHESION: case SF_FIELD_AVG_ADHESION: case SF_FIELD_CDA0ASAT:
+    case SF_BFIELD_POS:
+        return 3;
+    case SF_FIELD_AMCAMCP: return 2;
+    case SF_FIELD_LABEL: case SF_FIELD_RADIUS: case SF_FIELD_MASS: case SF_FIELD_DENSITY: case SF_FIELD_PRESSURE:
+    case SF_FIELD_VOIDAGE: case SF_FIELD_SATURATION: case SF_FIELD_MAX_SATURATION: case SF_FIELD_ID:
+    case SF_FIELD_KEY: case SF_BFIELD_LABEL: case SF_BFIELD_VOLUME:
+        return 1;
+    default: return 0;
+    }
+}
+
+sf_status ensureStage(sf_handle* h, size_t bytes) {
+    if (h->stageBytes >= bytes) return SF_OK;
+    if (h->stage) cudaFree(h->stage);
+    h->stage = nullptr;
+    h->stageBytes = 0;
+    if (h->cuda(cudaMalloc(&h->stage, bytes), "cudaMalloc staging")) return SF_ERR_CUDA;
+    h->stageBytes = bytes;
+    return SF_OK;
+}
+
+__global__ void kGetBoundary(int field, int n, int bOff, const float4* __restrict__ bpos, const int* __restrict__ bl,
+                             void* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 b = bpos[bOff + i];
+    float* f = static_cast<float*>(out);
+    if (field == SF_BFIELD_POS) {
+        f[3 * i] = b.x;
+        f[3 * i + 1] = b.y;
+        f[3 * i + 2] = b.z;
+    } else if (field == SF_BFIELD_LABEL) {
+        static_cast<int*>(out)[i] = bl[bOff + i];
+    } else {
+        f[i] = fabsf(b.w);
+    }
+}
+
+}  // namespace
+
+sf_status sf_get_field(sf_handle* h, int32_t scene, int32_t field, int32_t order, void* dst, int64_t count,
+                       int32_t dst_on_device) {
+    if (!h || !dst || scene < 0 || scene >= h->nScenes) return SF_ERR_INVALID;
+    const int w = fieldWidth(field);
+    if (w == 0) return h->fail(SF_ERR_INVALID, "unknown field");
+    if (order != SF_ORDER_SORTED && order != SF_ORDER_ID) return h->fail(SF_ERR_INVALID, "unknown order");
+    const SceneDev& S = h->hScenes[scene];
+    const bool bfield = field >= SF_BFIELD_POS;
+    const int64_t n = bfield ? S.nb : h->n[scene];
+    if (count != n) return h->fail(SF_ERR_INVALID, "count must equal the scene's particle count");
+    const size_t bytes = size_t(n) * size_t(w) * 4;
+    if (n == 0) return SF_OK;
+    void* target = dst;
+    if (!dst_on_device) {
+        if (ensureStage(h, bytes)) return SF_ERR_CUDA;
+        target = h->stage;
+    }
+    const int blocks = int((n + 255) / 256);
+    if (bfield) {
+        kGetBoundary<<<blocks, 256, 0, h->stream>>>(field, int(n), S.b_off, h->bpos, h->blabel, target);
+    } else {
+        const int c = h->cur;
+        kGetField<<<blocks, 256, 0, h->stream>>>(field, int(n), S.slot_off, S.cell_off, order, h->pos[c], h->vel[c],
+                                                 h->col[c], h->mat[c], h->amc[c], h->pid[c], h->aux, h->flow,
+                                                 h->adh, h->avgadh, h->drag, h->acc, h->sorted ? h->sortedKeys : nullptr,
+                                                 target);
+    }
+    if (h->cuda(cudaGetLastError(), "get_field launch")) return SF_ERR_CUDA;
+    if (!dst_on_device) {
+        if (h->cuda(cudaMemcpyAsync(dst, h->stage, bytes, cudaMemcpyDeviceToHost, h->stream), "get_field D2H"))
+            return SF_ERR_CUDA;
+        return h->cuda(cudaStreamSynchronize(h->stream), "get_field sync");
+    }
+    return SF_OK;
+}
+
+sf_status sf_set_field(sf_handle* h, int32_t scene, int32_t field, int32_t order, const void* src, int64_t count,
+                       int32_t src_on_device) {
+    if (!h || !src || scene < 0 || scene >= h->nScenes) return SF_ERR_INVALID;
+    const int w = fieldWidth(field);
+    if (w == 0 || field >= SF_BFIELD_POS || field == SF_FIELD_ID || field == SF_FIELD_KEY)
+        return h->fail(SF_ERR_INVALID, "field cannot be set");
+    if (order != SF_ORDER_SORTED && order != SF_ORDER_ID) return h->fail(SF_ERR_INVALID, "unknown order");
+    const SceneDev& S = h->hScenes[scene];
+    const int64_t n = h->n[scene];
+    if (count != n) return h->fail(SF_ERR_INVALID, "count must equal the scene's particle count");
+    if (n == 0) return SF_OK;
+    const size_t bytes = size_t(n) * size_t(w) * 4;
+    const void* from = src;
+    if (!src_on_device) {
+        if (ensureStage(h, bytes)) return SF_ERR_CUDA;
+        if (h->cuda(cudaMemcpyAsync(h->stage, src, bytes, cudaMemcpyHostToDevice, h->stream), "set_field H2D"))
+            return SF_ERR_CUDA;
+        from = h->stage;
+    }
+    const int c = h->cur;
+    kSetField<<<int((n + 255) / 256), 256, 0, h->stream>>>(field, int(n), S.slot_off, order, h->pos[c], h->vel[c],
+                                                           h->col[c], h->mat[c], h->amc[c], h->pid[c], h->aux,
+                                                           h->flow, h->adh, h->avgadh, h->drag, h->acc, from);
+    if (h->cuda(cudaGetLastError(), "set_field launch")) return SF_ERR_CUDA;
+    if (!src_on_device) return h->cuda(cudaStreamSynchronize(h->stream), "set_field sync");
+    return SF_OK;
+}
+
+sf_status sf_get_cell_table(sf_handle* h, int32_t scene, int32_t which, int64_t* dst, int64_t count) {
+    if (!h || !dst || scene < 0 || scene >= h->nScenes || (which != 0 && which != 1)) return SF_ERR_INVALID;
+    const SceneDev& S = h->hScenes[scene];
+    if (count != int64_t(S.ncell) + 1) return h->fail(SF_ERR_INVALID, "count must be G + 1");
+    if (which == 0 && !h->sorted) return h->fail(SF_ERR_INVALID, "no cell table before the first sort");
+    std::vector<unsigned> t(static_cast<size_t>(count));
+    if (h->cuda(cudaMemcpyAsync(t.data(), (which ? h->bcs : h->cs) + S.cell_off, sizeof(unsigned) * t.size(),
+                                cudaMemcpyDeviceToHost, h->stream),
+                "cell table D2H") ||
+        h->cuda(cudaStreamSynchronize(h->stream), "cell table sync"))
+        return SF_ERR_CUDA;
+    const int64_t base = which ? S.b_off : S.slot_off;
+    for (size_t c = 0; c < t.size(); ++c) dst[c] = int64_t(t[c]) - base;
+    return SF_OK;
+}
+
+sf_status sf_get_grid(const sf_handle* h, int32_t scene, int32_t grid_size[3], int64_t* n_cells) {
+    if (!h || scene < 0 || scene >= h->nScenes) return SF_ERR_INVALID;
+    const SceneDev& S = h->hScenes[scene];
+    if (grid_size) {
+        grid_size[0] = S.gx;
+        grid_size[1] = S.gy;
+        grid_size[2] = S.gz;
+    }
+    if (n_cells) *n_cells = S.ncell;
+    return SF_OK;
+}
+
+sf_status sf_size(const sf_handle* h, int32_t scene, int64_t* n, int64_t* capacity) {
+    if (!h || scene < 0 || scene >= h->nScenes) return SF_ERR_INVALID;
+    if (n) *n = h->n[scene];
+    if (capacity) *capacity = h->capUser[scene];
+    return SF_OK;
+}
+
+sf_status sf_num_scenes(const sf_handle* h, int32_t* n_scenes) {
+    if (!h || !n_scenes) return SF_ERR_INVALID;
+    *n_scenes = h->nScenes;
+    return SF_OK;
+}
+
+sf_status sf_num_substeps(sf_handle* h, int32_t scene, int64_t* n_sub) {
+    if (!h || !n_sub || scene < 0 || scene >= h->nScenes) return SF_ERR_INVALID;
+    SceneState s;
+    if (h->cuda(cudaMemcpyAsync(&s, h->dState + scene, sizeof(SceneState), cudaMemcpyDeviceToHost, h->stream),
+                "read state") ||
+        h->cuda(cudaStreamSynchronize(h->stream), "sync"))
+        return SF_ERR_CUDA;
+    *n_sub = s.n_sub;
+    return SF_OK;
+}
+
+sf_status sf_add_sph_particles(sf_handle* h, int32_t scene, const float* pos3, int64_t n, const float col[3],
+                               const float vel[3], float mass, float radius) {
+    if (!h || scene < 0 || scene >= h->nScenes || n < 0 || (n > 0 && !pos3) || !col || !vel)
+        return SF_ERR_INVALID;
+    if (!(mass > 0.f)) return h->fail(SF_ERR_INVALID, "mass must be > 0");
+    // cuda_sf_particles.cu:54-58: refuse when Size() + num >= MaxSize()
+    if (h->n[scene] + n >= h->capUser[scene])
+        return h->fail(SF_ERR_CAPACITY, "Current SPH particles numbers exceed maximum particles.");
+    if (n == 0) return SF_OK;
+    const SceneDev& S = h->hScenes[scene];
+    std::vector<float4> p(static_cast<size_t>(n)), v(static_cast<size_t>(n)), c(static_cast<size_t>(n)), m(static_cast<size_t>(n));
+    std::vector<float2> a(static_cast<size_t>(n), make_float2(0.f, 0.f));
+    std::vector<int> id(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) {
+        p[i] = make_float4(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2], mass);
+        v[i] = make_float4(vel[0], vel[1], vel[2], 0.f);
+        c[i] = make_float4(col[0], col[1], col[2], 0.f);
+        m[i] = make_float4(0.f, 0.f, 0.f, radius);
+        id[i] = int(h->nextId[scene] + i);
+    }
+    const size_t off = size_t(S.slot_off + h->n[scene]);
+    const int k = h->cur;
+    auto up = [&](void* d, const void* s, size_t b) {
+        return h->cuda(cudaMemcpyAsync(d, s, b, cudaMemcpyHostToDevice, h->stream), "add particles H2D");
+    };
+    if (up(h->pos[k] + off, p.data(), sizeof(float4) * n) || up(h->vel[k] + off, v.data(), sizeof(float4) * n) ||
+        up(h->col[k] + off, c.data(), sizeof(float4) * n) || up(h->mat[k] + off, m.data(), sizeof(float4) * n) ||
+        up(h->amc[k] + off, a.data(), sizeof(float2) * n) || up(h->pid[k] + off, id.data(), sizeof(int) * n) ||
+        h->cuda(cudaStreamSynchronize(h->stream), "add particles sync"))
+        return SF_ERR_CUDA;
+    h->n[scene] += n;
+    h->nextId[scene] += n;
+    return SF_OK;
+}
+
+sf_status sf_check_error(sf_handle* h, uint32_t* flags) {
+    if (!h || !flags) return SF_ERR_INVALID;
+    unsigned v = 0;
+    if (h->cuda(cudaMemcpyAsync(&v, h->dErr, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream), "read error") ||
+        h->cuda(cudaMemsetAsync(h->dErr, 0, sizeof(unsigned), h->stream), "clear error") ||
+        h->cuda(cudaStreamSynchronize(h->stream), "sync"))
+        return SF_ERR_CUDA;
+    *flags = v;
+    return v ? SF_ERR_DEVICE : SF_OK;
+}
+
+sf_status sf_synchronize(sf_handle* h) {
+    if (!h) return SF_ERR_INVALID;
+    return h->cuda(cudaStreamSynchronize(h->stream), "sf_synchronize");
+}
+
+sf_status sf_launch_count(const sf_handle* h, int64_t* launches) {
+    if (!h || !launches) return SF_ERR_INVALID;
+    *launches = h->launches;
+    return SF_OK;
+}
+
+sf_status sf_set_tuning(sf_handle* h, int32_t block_size, int32_t items_per_thread) {
+    if (!h) return SF_ERR_INVALID;
+    if ((block_size != 0 && block_size != kSlotAlign) || (items_per_thread != 0 && items_per_thread != 1))
+        return h->fail(SF_ERR_UNSUPPORTED, "this build runs the passes with 256 threads, one slot each");
+    return SF_OK;
+}
+
+const char* sf_last_error_string(const sf_handle* h) { return h ? h->err.c_str() : g_createError.c_str(); }
+
+}  // extern "C"

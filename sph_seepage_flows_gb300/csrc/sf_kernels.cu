@@ -1,0 +1,579 @@
+// Neighbor passes, integrator and boundary-volume kernels of the GB300
+// seepage-flow substep. One thread per slot; each block of kSlotAlign slots
+// belongs to one scene (blockScene). Every pass is a gather: a thread writes
+// only its own slot, so no pass needs atomics except the per-scene max |acc|.
+//
+// The neighbor loops visit the 27 cells in the reference order
+// (m = 0..26, dx-major, e.g. cuda_sph_sf_solver_gpu.cuh:468-477) and, inside
+// a cell, run the reference's sub-loops in the reference order, so every
+// accumulator sums the same terms in the same order as the reference kernel.
+// Pairs farther apart than the interaction reach (all of whose terms are
+// exactly +0 in the reference) are skipped before any term is evaluated.
+#include "sf_device.cuh"
+#include "sf_kernels.h"
+
+namespace sfg {
+
+#define SF_SLOT_PROLOGUE                                                   \
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;                \
+    const int sid = blockScene[(blockIdx.x * blockDim.x) / kSlotAlign];    \
+    const SceneDev& S = scenes[sid];
+
+// 27-cell stencil of the reference, with the global cell index of cell m.
+template <typename F>
+__device__ __forceinline__ void forEachCell(const SceneDev& S, int3 c, F&& f) {
+#pragma unroll 1
+    for (int dx = -1; dx <= 1; ++dx) {
+        const int x = c.x + dx;
+        if (x < 0 || x >= S.gx) continue;
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int y = c.y + dy;
+            if (y < 0 || y >= S.gy) continue;
+            const int base = S.cell_off + (x * S.gy + y) * S.gz;
+#pragma unroll 1
+            for (int dz = -1; dz <= 1; ++dz) {
+                const int z = c.z + dz;
+                if (z < 0 || z >= S.gz) continue;
+                f(base + z);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ bool inReach(const SceneDev& S, float3 d) { return dot3(d, d) < S.reach2; }
+
+// ---------------------------------------------------------------------- keys
+// Pos2GridHash (helper_thrust.cuh:66-89) into the global cell space; parking
+// slots get the scene's parking cell.
+__global__ void kKeys(const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene,
+                      const float4* __restrict__ pos4, unsigned int* __restrict__ keys, unsigned int* errWord) {
+    SF_SLOT_PROLOGUE
+    const float4 p = pos4[slot];
+    unsigned int k;
+    if (p.w == 0.f) {
+        k = unsigned(S.cell_off + S.ncell);
+    } else {
+        const float3 q = xyz(p);
+        if (!(isfinite(q.x) && isfinite(q.y) && isfinite(q.z))) atomicOr(errWord, 1u);
+        k = unsigned(S.cell_off + localHash(S, cellOf(S, q)));
+    }
+    keys[slot] = k;
+}
+
+// ----------------------------------------------------------- boundary volume
+// ComputeBoundaryVolume_CUDA (cuda_sph_system_gpu.cuh:19-67): V_b = 1 / max(sum_{j != i} W, eps).
+__global__ void kBoundaryVolume(const SceneDev* __restrict__ scenes, int sid, float4* __restrict__ bpos4,
+                                const int* __restrict__ blabel, const unsigned int* __restrict__ bcs) {
+    const SceneDev& S = scenes[sid];
+    const int i = S.b_off + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.b_off + S.nb) return;
+    const float3 pi = xyz(bpos4[i]);
+    float v = 0.f;
+    forEachCell(S, cellOf(S, pi), [&](int cell) {
+        for (unsigned j = bcs[cell]; j < bcs[cell + 1]; ++j)
+            if (int(j) != i) v += poly6(S, len3(pi - xyz(bpos4[j])));
+    });
+    const float vol = 1.f / fmaxf(v, kEps);
+    bpos4[i].w = blabel[i] == 1 ? -vol : vol;
+}
+
+// ------------------------------------------------------------ density stage
+// ComputeSFDensity_CUDA + ComputeSFFluidDensity + ComputeBoundaryDensity
+// (cuda_sph_sf_solver_gpu.cuh:408-480, cuda_sph_solver_common_gpu.cuh:70-87)
+// fused with ComputeSFPressureByTait_CUDA (cuda_wcsph_sf_solver_gpu.cuh:19-44)
+// or ComputeSFPressure_CUDA (cuda_sph_sf_solver_gpu.cuh:482-508).
+__global__ void kDensity(const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene,
+                         SceneState* __restrict__ state, const unsigned int* __restrict__ cs,
+                         const unsigned int* __restrict__ bcs, const float4* __restrict__ pos4,
+                         const float4* __restrict__ bpos4, float4* __restrict__ vel4, float4* __restrict__ aux4) {
+    SF_SLOT_PROLOGUE
+    if (slot == S.slot_off) state[sid].amax_bits = 0u;
+    const float4 pi4 = pos4[slot];
+    if (pi4.w == 0.f) return;
+    float density, pressure = 0.f;
+    if (pi4.w < 0.f) {
+        density = S.rho1;
+    } else {
+        const float3 pi = xyz(pi4);
+        const float mi = pi4.w;
+        float d = mi * S.W0;
+        forEachCell(S, cellOf(S, pi), [&](int cell) {
+            for (unsigned j = cs[cell]; j < cs[cell + 1]; ++j) {
+                const float4 pj = pos4[j];
+                if (pj.w > 0.f) {  // label[i] == label[j] (water)
+                    const float3 dij = pi - xyz(pj);
+                    if (inReach(S, dij)) d += pj.w * poly6(S, len3(dij));
+                }
+            }
+            for (unsigned j = bcs[cell]; j < bcs[cell + 1]; ++j) {
+                const float4 bj = bpos4[j];
+                const float3 dij = pi - xyz(bj);
+                if (inReach(S, dij)) d += S.rho0 * fabsf(bj.w) * poly6(S, len3(dij));
+            }
+        });
+        density = d;
+        if (S.tait) {
+            pressure = S.stiff * (powf(density / S.rho0, 7.f) - 1.f);
+            if (pressure < 0.f) pressure *= S.neg_scale;
+        } else {
+            pressure = S.stiff * (density - S.rho0);
+            if (pressure < 0.f) pressure *= 1.f;
+        }
+    }
+    vel4[slot].w = density;
+    aux4[slot].x = pressure;
+}
+
+// ------------------------------------------------------------ avg-flow stage
+// ComputeSFAvgFlow_CUDA with ComputeSFSandVolume and ComputeSFAvgFlow
+// (cuda_sph_sf_solver_gpu.cuh:111-173, 510-572). The two sub-loops feed
+// disjoint accumulators, so one sweep over the cell keeps every sum's order.
+__global__ void kAvgFlow(const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene,
+                         const unsigned int* __restrict__ cs, const float4* __restrict__ pos4,
+                         const float4* __restrict__ vel4, float4* __restrict__ aux4, float4* __restrict__ flow4) {
+    SF_SLOT_PROLOGUE
+    const float4 pi4 = pos4[slot];
+    if (pi4.w == 0.f) return;
+    const float3 pi = xyz(pi4);
+    const bool sandI = pi4.w < 0.f;
+    float v_s = 0.f, v_w = 0.f, sand_volume = 0.f;
+    float3 avg_s = mk3(0.f, 0.f, 0.f), avg_w = avg_s;
+    forEachCell(S, cellOf(S, pi), [&](int cell) {
+        for (unsigned j = cs[cell]; j < cs[cell + 1]; ++j) {
+            const float4 pj = pos4[j];
+            const float3 dij = pi - xyz(pj);
+            if (!inReach(S, dij)) continue;
+            const float4 vj4 = vel4[j];
+            const bool sandJ = pj.w < 0.f;
+            const float mj = fabsf(pj.w);
+            const float wij = poly6(S, len3(dij));
+            if (sandJ && vj4.w != 0.f) sand_volume += mj / vj4.w * wij;
+            const float vj = mj / vj4.w;
+            if (sandI && !sandJ) {
+                avg_s += xyz(vj4) * vj * wij;
+                v_s += vj * wij;
+            } else if (!sandI && sandJ) {
+                avg_w += xyz(vj4) * vj * wij;
+                v_w += vj * wij;
+            }
+        }
+    });
+    float3 avg;
+    if (!sandI && v_w != 0.f)
+        avg = avg_w / v_w;
+    else if (sandI && v_s != 0.f)
+        avg = avg_s / v_s;
+    else
+        avg = mk3(0.f, 0.f, 0.f);
+    flow4[slot] = make_float4(avg.x, avg.y, avg.z, 0.f);
+    float4 a = aux4[slot];
+    a.y = 1.f - sand_volume;
+    a.z = v_s;
+    a.w = a.y;  // the reference's voidage array holds the fluid voidage until the sand pass
+    aux4[slot] = a;
+}
+
+// ------------------------------------------------ voidage / adhesion stage
+// Sand: ComputeSFSandVoidage_CUDA (cuda_sph_sf_solver_gpu.cuh:209-238,
+// 680-721) and ComputeSFWetSandColor_CUDA (952-977). Water: the SF or MULTI
+// water adhesion kernel (175-207, 574-678). Reads the fluid voidage (aux.y)
+// of water neighbours and writes the final voidage (aux.w) of every slot.
+__global__ void kVoidageAdhesion(const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene,
+                                 const unsigned int* __restrict__ cs, const float4* __restrict__ pos4,
+                                 const float4* __restrict__ vel4, float4* __restrict__ aux4,
+                                 float4* __restrict__ adh4, float4* __restrict__ avgadh4,
+                                 float4* __restrict__ col4) {
+    SF_SLOT_PROLOGUE
+    const float4 pi4 = pos4[slot];
+    if (pi4.w == 0.f) return;
+    const float3 pi = xyz(pi4);
+    if (pi4.w < 0.f) {
+        const float sat = aux4[slot].z;
+        float num = 0.f, den = 0.f;
+        forEachCell(S, cellOf(S, pi), [&](int cell) {
+            for (unsigned j = cs[cell]; j < cs[cell + 1]; ++j) {
+                const float4 pj = pos4[j];
+                if (!(pj.w > 0.f)) continue;
+                const float3 dij = pi - xyz(pj);
+                if (!inReach(S, dij)) continue;
+                const float vj = pj.w / vel4[j].w;
+                const float wij = poly6(S, len3(dij));
+                num += aux4[j].y * vj * wij;
+                den += vj * wij;
+            }
+        });
+        aux4[slot].w = den != 0.f ? num / den : 0.f;
+        // wet-sand colour ratchet
+        float4 c = col4[slot];
+        if (c.w < sat) {
+            c.x = S.dry[0] + (S.wet[0] - S.dry[0]) * sat;
+            c.y = S.dry[1] + (S.wet[1] - S.dry[1]) * sat;
+            c.z = S.dry[2] + (S.wet[2] - S.dry[2]) * sat;
+            c.w = sat;
+            col4[slot] = c;
+        }
+        adh4[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+        avgadh4[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {
+        const float mi = pi4.w;
+        float v_s = 0.f;
+        float3 ad = mk3(0.f, 0.f, 0.f);
+        forEachCell(S, cellOf(S, pi), [&](int cell) {
+            for (unsigned j = cs[cell]; j < cs[cell + 1]; ++j) {
+                const float4 pj = pos4[j];
+                if (!(pj.w < 0.f)) continue;
+                const float3 dpij = pi - xyz(pj);
+                if (!inReach(S, dpij)) continue;
+                const float ldp = len3(dpij);
+                const float wij = poly6(S, ldp);
+                const float adij = adhesionSpline(S, ldp);
+                const float mj = -pj.w;
+                ad += bezier(S.adhG, aux4[j].z) * mi * mj * adij * dpij / fmaxf(kEps, ldp);
+                const float vj = mj / vel4[j].w;
+                v_s += vj * wij;
+            }
+        });
+        adh4[slot] = make_float4(ad.x, ad.y, ad.z, 0.f);
+        const float3 avg = v_s != 0.f ? ad / v_s : mk3(0.f, 0.f, 0.f);
+        avgadh4[slot] = make_float4(avg.x, avg.y, avg.z, 0.f);
+    }
+}
+
+// ---------------------------------------------------------- sand momentum
+// Compute[Multi]SFSandLinearMomentum_CUDA (cuda_sph_sf_solver_gpu.cuh:723-897)
+// with the DEM, capillary, buoyancy, adhesion and boundary-DEM sub-loops per
+// cell (21-109, 240-273, 314-341) and ComputeDemWorldBoundaryForces
+// (cuda_dem_solver_common_gpu.cuh:132-199). acc = g + 2 (f + df) / m.
+__global__ void kSandMomentum(const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene,
+                              const unsigned int* __restrict__ cs, const unsigned int* __restrict__ bcs,
+                              const float4* __restrict__ pos4, const float4* __restrict__ vel4,
+                              const float4* __restrict__ aux4, const float4* __restrict__ flow4,
+                              const float4* __restrict__ avgadh4, const float4* __restrict__ mat4,
+                              const float4* __restrict__ bpos4, float4* __restrict__ drag4,
+                              float4* __restrict__ acc4) {
+    SF_SLOT_PROLOGUE
+    const float4 pi4 = pos4[slot];
+    if (!(pi4.w < 0.f)) {
+        if (pi4.w > 0.f) drag4[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    const float3 pi = xyz(pi4);
+    const float mi = -pi4.w;
+    const float4 vi4 = vel4[slot];
+    const float3 vi = xyz(vi4);
+    const float di = vi4.w;
+    const float4 ai = aux4[slot];
+    float v_w = 0.f;
+    float3 f = mk3(0.f, 0.f, 0.f), df = f;
+    forEachCell(S, cellOf(S, pi), [&](int cell) {
+        const unsigned j0 = cs[cell], j1 = cs[cell + 1];
+        // ComputeSFUniRadiusDemForces (21-50)
+        for (unsigned j = j0; j < j1; ++j) {
+            const float4 pj = pos4[j];
+            if (!(pj.w < 0.f) || int(j) == slot) continue;
+            const float3 dij = xyz(pj) - pi;
+            if (!inReach(S, dij)) continue;
+            f += demForce(dij, xyz(vel4[j]) - vi, S.rij2, S.kn, S.ks, S.tan2);
+        }
+        // ComputeSFUniRadiusDemCapillaryForces (83-109)
+        for (unsigned j = j0; j < j1; ++j) {
+            const float4 pj = pos4[j];
+            if (!(pj.w < 0.f) || int(j) == slot) continue;
+            const float3 dij = xyz(pj) - pi;
+            if (!inReach(S, dij)) continue;
+            f += capillaryForce(S, dij, (ai.z + aux4[j].z) / 2.f);
+        }
+        // ComputeSFSandBuoyancyForces (240-273)
+        for (unsigned j = j0; j < j1; ++j) {
+            const float4 pj = pos4[j];
+            if (!(pj.w > 0.f)) continue;
+            const float3 dij = pi - xyz(pj);
+            if (!inReach(S, dij)) continue;
+            const float4 aj = aux4[j];
+            if (!(aj.w > 0.f && aj.w <= 1.f)) continue;
+            const float dj = vel4[j].w / fmaxf(kEps, aj.w);
+            const float wij = poly6(S, len3(dij));
+            const float3 nab = spikyGrad(S, dij);
+            v_w += pj.w / dj * wij;
+            f += -mi * pj.w * aj.x / fmaxf(kEps, di * dj) * nab;
+        }
+        // ComputeSFSandAdhesionTerm (314-341)
+        for (unsigned j = j0; j < j1; ++j) {
+            const float4 pj = pos4[j];
+            if (!(pj.w > 0.f)) continue;
+            const float3 dij = pi - xyz(pj);
+            if (!inReach(S, dij)) continue;
+            const float wij = poly6(S, len3(dij));
+            const float v = mi / fmaxf(kEps, di);
+            f += wij * v * xyz(avgadh4[j]);
+        }
+        // ComputeSFUniRadiusDemBoundaryForces (52-81): boundary particles with label 1
+        for (unsigned j = bcs[cell]; j < bcs[cell + 1]; ++j) {
+            const float4 bj = bpos4[j];
+            if (!(bj.w < 0.f)) continue;
+            const float3 dij = pi - xyz(bj);
+            if (!inReach(S, dij)) continue;
+            f += demForce(dij, mk3(-vi.x, -vi.y, -vi.z), S.rij2, S.kn, S.ks, S.tan2);
+        }
+    });
+    // ComputeDemWorldBoundaryForces; the z-min wall tests 2 * rij (DEM:191)
+    {
+        const float rij = S.wall_rij;
+        const float3 nv = -vi;
+        if (pi.x > S.hpx - rij) f += demForce(mk3(1.f, 0.f, 0.f) * fabsf(pi.x - S.hpx), nv, rij, S.kn, S.ks, S.tan2);
+        if (pi.x < S.lpx + rij) f += demForce(mk3(-1.f, 0.f, 0.f) * fabsf(pi.x - S.lpx), nv, rij, S.kn, S.ks, S.tan2);
+        if (pi.y > S.hpy - rij) f += demForce(mk3(0.f, 1.f, 0.f) * fabsf(pi.y - S.hpy), nv, rij, S.kn, S.ks, S.tan2);
+        if (pi.y < S.lpy + rij) f += demForce(mk3(0.f, -1.f, 0.f) * fabsf(pi.y - S.lpy), nv, rij, S.kn, S.ks, S.tan2);
+        if (pi.z > S.hpz - rij) f += demForce(mk3(0.f, 0.f, 1.f) * fabsf(pi.z - S.hpz), nv, rij, S.kn, S.ks, S.tan2);
+        if (pi.z < S.lpz + 2.f * rij)
+            f += demForce(mk3(0.f, 0.f, -1.f) * fabsf(pi.z - S.lpz), nv, rij, S.kn, S.ks, S.tan2);
+    }
+    const float eps_i = ai.w;
+    if (eps_i < 1.f && eps_i > 0.f) {
+        const float cd = S.multi ? mat4[slot].x : S.cd;
+        const float dragCoeff = cd * powf(eps_i, 3.f) / powf(1.f - eps_i, 2.f);
+        if (dragCoeff != 0.f)
+            df = S.grav_abs * S.rho0 * powf(eps_i, 2.f) / dragCoeff * (xyz(flow4[slot]) - vi) * mi / di;
+    }
+    const float3 avgDrag = v_w != 0.f ? df / v_w : mk3(0.f, 0.f, 0.f);
+    drag4[slot] = make_float4(avgDrag.x, avgDrag.y, avgDrag.z, 0.f);
+    const float3 g = mk3(0.f, 0.f, 0.f) + mk3(S.gvx, S.gvy, S.gvz);
+    const float3 a = g + 2.f * (f + df) / mi;
+    acc4[slot] = make_float4(a.x, a.y, a.z, 0.f);
+}
+
+// --------------------------------------------------------- water momentum
+// ComputeSFWaterLinearMomentum_CUDA (cuda_sph_sf_solver_gpu.cuh:899-950) with
+// the pressure (343-369), artificial viscosity (371-406), seepage (275-312),
+// boundary pressure and boundary viscosity (cuda_sph_solver_common_gpu.cuh:
+// 89-139; called with rho0 as the particle density) sub-loops per cell.
+// acc = g + (a - F_adh / m). Every thread then contributes |acc| of its slot
+// (sand included) to the scene maximum (cuda_wcsph_sf_solver.cu:43-47).
+__global__ void kWaterMomentum(const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene,
+                               SceneState* __restrict__ state, const unsigned int* __restrict__ cs,
+                               const unsigned int* __restrict__ bcs, const float4* __restrict__ pos4,
+                               const float4* __restrict__ vel4, const float4* __restrict__ aux4,
+                               const float4* __restrict__ drag4, const float4* __restrict__ adh4,
+                               const float4* __restrict__ bpos4, float4* __restrict__ acc4,
+                               unsigned int* errWord) {
+    SF_SLOT_PROLOGUE
+    const float4 pi4 = pos4[slot];
+    float alen = 0.f;
+    if (pi4.w > 0.f) {
+        const float3 pi = xyz(pi4);
+        const float4 vi4 = vel4[slot];
+        const float3 vi = xyz(vi4);
+        const float4 ai4 = aux4[slot];
+        const float di = vi4.w / fmaxf(kEps, ai4.w);
+        const float pri = ai4.x;
+        const float pterm_i = pri / fmaxf(kEps, di * di);
+        float3 a = mk3(0.f, 0.f, 0.f);
+        forEachCell(S, cellOf(S, pi), [&](int cell) {
+            const unsigned j0 = cs[cell], j1 = cs[cell + 1];
+            // ComputeSFWaterPressureTerm (343-369)
+            for (unsigned j = j0; j < j1; ++j) {
+                const float4 pj = pos4[j];
+                if (!(pj.w > 0.f) || int(j) == slot) continue;
+                const float3 dij = pi - xyz(pj);
+                if (!inReach(S, dij)) continue;
+                const float4 aj = aux4[j];
+                const float dj = vel4[j].w / fmaxf(kEps, aj.w);
+                a += -pj.w * (pterm_i + aj.x / fmaxf(kEps, dj * dj)) * spikyGrad(S, dij);
+            }
+            // ComputeSFWaterArtificialViscosity (371-406)
+            for (unsigned j = j0; j < j1; ++j) {
+                const float4 pj = pos4[j];
+                if (!(pj.w > 0.f) || int(j) == slot) continue;
+                const float3 dpij = pi - xyz(pj);
+                if (!inReach(S, dpij)) continue;
+                const float4 vj4 = vel4[j];
+                const float3 dv = vi - xyz(vj4);
+                const float dd = dot3(dv, dpij);
+                if (dd < 0.f) {
+                    const float dj = vj4.w / fmaxf(kEps, aux4[j].w);
+                    const float pij = -S.nu / (di + dj) * (dd / (dot3(dpij, dpij) + kEps));
+                    a += -pj.w * pij * spikyGrad(S, dpij);
+                }
+            }
+            // ComputeSFWaterSeepageTerm (275-312)
+            for (unsigned j = j0; j < j1; ++j) {
+                const float4 pj = pos4[j];
+                if (!(pj.w < 0.f)) continue;
+                const float3 dij = pi - xyz(pj);
+                if (!inReach(S, dij)) continue;
+                const float dj = vel4[j].w;
+                const float wij = poly6(S, len3(dij));
+                const float3 nab = spikyGrad(S, dij);
+                const float3 buoy = pj.w * pri / fmaxf(kEps, di * dj) * nab;  // -m_j with m_j = -w
+                const float3 drag = -wij / di * xyz(drag4[j]);
+                a += buoy + drag;
+            }
+            // ComputeBoundaryPressure / ComputeBoundaryViscosity (rho0 as density)
+            const unsigned b0 = bcs[cell], b1 = bcs[cell + 1];
+            for (unsigned j = b0; j < b1; ++j) {
+                const float4 bj = bpos4[j];
+                const float3 dij = pi - xyz(bj);
+                if (!inReach(S, dij)) continue;
+                a += -S.rho0 * fabsf(bj.w) * (pri / fmaxf(kEps, S.rho0 * S.rho0)) * spikyGrad(S, dij);
+            }
+            for (unsigned j = b0; j < b1; ++j) {
+                const float4 bj = bpos4[j];
+                const float3 dpij = pi - xyz(bj);
+                if (!inReach(S, dpij)) continue;
+                const float dd = dot3(vi, dpij);
+                if (dd < 0.f) {
+                    const float pij = -S.bnu / (2.f * S.rho0) * (dd / (dot3(dpij, dpij) + kEps));
+                    a += -fabsf(bj.w) * S.rho0 * pij * spikyGrad(S, dpij);
+                }
+            }
+        });
+        const float3 g = mk3(0.f, 0.f, 0.f) + mk3(S.gvx, S.gvy, S.gvz);
+        const float3 acc = g + (a - xyz(adh4[slot]) / pi4.w);
+        acc4[slot] = make_float4(acc.x, acc.y, acc.z, 0.f);
+        alen = len3(acc);
+    } else if (pi4.w < 0.f) {
+        alen = len3(xyz(acc4[slot]));
+    }
+    if (!(alen <= 3.0e38f) && pi4.w != 0.f) atomicOr(errWord, 1u);
+    // block max of |acc| (non-negative floats order like their bit patterns)
+    float m = (alen == alen) ? alen : 0.f;
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ float wmax[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) wmax[warp] = m;
+    __syncthreads();
+    if (warp == 0) {
+        m = lane < int(blockDim.x >> 5) ? wmax[lane] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0 && m > 0.f) atomicMax(&state[sid].amax_bits, __float_as_uint(m));
+    }
+}
+
+// -------------------------------------------------------------- integrate
+// ComputeSubTimeStepsByCFL (cuda_wcsph_sf_solver.cu:35-58) on the device,
+// then CudaSFParticles::Advect with AccDampingForSand (cuda_sf_particles.cu:
+// 18-48, cuda_sf_particles.cuh:19-40) and SFWaterBoundaryConstrain_CUDA
+// (cuda_sph_sf_solver_gpu.cuh:979-1074). adaptive: timeArg is the render
+// interval and dt = timeArg / N_sub; otherwise dt = timeArg.
+__device__ __forceinline__ long long cflSubsteps(const SceneDev& S, float amax, float T) {
+    if (!S.wcsph) {
+        const float q = T / S.params_dt;
+        return q >= 9.2e18f ? (long long)9.2e18f : (long long)q;
+    }
+    const float maxForce = amax * S.cfl_mass;
+    const float byForce = 0.25f * sqrtf(S.cfl_hm / maxForce);
+    const float inner = byForce < S.cfl_by_speed ? byForce : S.cfl_by_speed;  // std::min
+    const float scaled = S.cfl_scale * inner;
+    const float desired = S.params_dt < scaled ? S.params_dt : scaled;
+    const float q = T / desired;
+    return q >= 9.2e18f ? (long long)9.2e18f : (long long)q;
+}
+
+__global__ void kIntegrate(const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene,
+                           SceneState* __restrict__ state, float timeArg, int adaptive,
+                           const unsigned int* __restrict__ bcs, const float4* __restrict__ bpos4,
+                           float4* __restrict__ pos4, float4* __restrict__ vel4, float4* __restrict__ acc4,
+                           float4* __restrict__ adh4, float4* __restrict__ avgadh4) {
+    SF_SLOT_PROLOGUE
+    float dt = timeArg;
+    if (adaptive) {
+        const long long ns = cflSubsteps(S, __uint_as_float(state[sid].amax_bits), timeArg);
+        dt = timeArg / float(ns);
+        if (slot == S.slot_off) {
+            state[sid].n_sub = ns;
+            state[sid].dt = dt;
+        }
+    } else if (slot == S.slot_off) {
+        state[sid].dt = dt;
+    }
+    float4 p4 = pos4[slot];
+    if (p4.w == 0.f) return;
+    float4 v4 = vel4[slot];
+    float3 a = xyz(acc4[slot]);
+    float3 v = xyz(v4);
+    if (p4.w < 0.f) {
+        const float3 q = a * (v + 0.5f * dt * a);
+        const float3 s = mk3(float(sgn1(q.x)), float(sgn1(q.y)), float(sgn1(q.z)));
+        a = a * (mk3(1.f, 1.f, 1.f) - S.damping * s);
+        acc4[slot] = make_float4(a.x, a.y, a.z, 0.f);
+    }
+    v = v + dt * a;
+    float3 p = xyz(p4) + dt * v;
+    if (p4.w > 0.f) {
+        const float r2 = 2.f * S.sph_radius;
+        float3 tp = p, tv = v;
+        if (tp.x > S.hpx - r2) { tp.x = S.hpx - r2; tv.x = fminf(tv.x, 0.f); }
+        if (tp.x < S.lpx + r2) { tp.x = S.lpx + r2; tv.x = fmaxf(tv.x, 0.f); }
+        if (tp.y > S.hpy - r2) { tp.y = S.hpy - r2; tv.y = fminf(tv.y, 0.f); }
+        if (tp.y < S.lpy + r2) { tp.y = S.lpy + r2; tv.y = fmaxf(tv.y, 0.f); }
+        if (tp.z > S.hpz - r2) { tp.z = S.hpz - r2; tv.z = fminf(tv.z, 0.f); }
+        if (tp.z < S.lpz + r2) { tp.z = S.lpz + r2; tv.z = fmaxf(tv.z, 0.f); }
+        forEachCell(S, cellOf(S, p), [&](int cell) {
+            for (unsigned j = bcs[cell]; j < bcs[cell + 1]; ++j) {
+                const float4 bj = bpos4[j];
+                if (!(bj.w < 0.f)) continue;
+                const float dpij = len3(p - xyz(bj));
+                const float overlap = dpij - r2;
+                if (overlap < 0.f) {
+                    const float3 nn = (p - xyz(bj)) / dpij;
+                    tv = tv * 0.f;
+                    tp += nn * -overlap;
+                }
+            }
+        });
+        p = tp;
+        v = tv;
+    }
+    pos4[slot] = make_float4(p.x, p.y, p.z, p4.w);
+    vel4[slot] = make_float4(v.x, v.y, v.z, v4.w);
+    // the two thrust::fill clears of cuda_sph_sf_solver.cu:384-385
+    adh4[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+    avgadh4[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// ------------------------------------------------------------ launchers
+void launchKeys(const LaunchCtx& c, const float4* pos4, unsigned int* keys) {
+    kKeys<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, pos4, keys, c.errWord);
+}
+
+void launchBoundaryVolume(const LaunchCtx& c, int sid, int nb, float4* bpos4, const int* blabel,
+                          const unsigned int* bcs) {
+    if (nb <= 0) return;
+    kBoundaryVolume<<<(nb + 255) / 256, 256, 0, c.stream>>>(c.scenes, sid, bpos4, blabel, bcs);
+}
+
+void launchDensity(const LaunchCtx& c, const PassBuffers& b) {
+    kDensity<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, c.state, b.cs, b.bcs, b.pos4,
+                                                        b.bpos4, b.vel4, b.aux4);
+}
+
+void launchAvgFlow(const LaunchCtx& c, const PassBuffers& b) {
+    kAvgFlow<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, b.cs, b.pos4, b.vel4, b.aux4,
+                                                        b.flow4);
+}
+
+void launchVoidageAdhesion(const LaunchCtx& c, const PassBuffers& b) {
+    kVoidageAdhesion<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, b.cs, b.pos4, b.vel4,
+                                                                b.aux4, b.adh4, b.avgadh4, b.col4);
+}
+
+void launchSandMomentum(const LaunchCtx& c, const PassBuffers& b) {
+    kSandMomentum<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, b.cs, b.bcs, b.pos4, b.vel4,
+                                                             b.aux4, b.flow4, b.avgadh4, b.mat4, b.bpos4, b.drag4,
+                                                             b.acc4);
+}
+
+void launchWaterMomentum(const LaunchCtx& c, const PassBuffers& b) {
+    kWaterMomentum<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, c.state, b.cs, b.bcs,
+                                                              b.pos4, b.vel4, b.aux4, b.drag4, b.adh4, b.bpos4,
+                                                              b.acc4, c.errWord);
+}
+
+void launchIntegrate(const LaunchCtx& c, const PassBuffers& b, float timeArg, int adaptive) {
+    kIntegrate<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, c.state, timeArg, adaptive,
+                                                          b.bcs, b.bpos4, b.pos4, b.vel4, b.acc4, b.adh4,
+                                                          b.avgadh4);
+}
+
+}  // namespace sfg

@@ -1,0 +1,71 @@
+// Host-side launch interface of the substep kernels (sf_kernels.cu, sf_sort.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sfg {
+
+struct SceneDev;
+struct SceneState;
+
+// Launch context shared by all passes of one handle.
+struct LaunchCtx {
+    cudaStream_t stream;
+    const SceneDev* scenes;   // device array [n_scenes]
+    const int* blockScene;    // device array [slotBlocks]: scene of each kSlotAlign block
+    SceneState* state;        // device array [n_scenes]
+    unsigned int* errWord;    // device error word
+    int slotBlocks;           // total slots / kSlotAlign
+};
+
+// Device buffers the neighbor passes read and write (current sort order).
+struct PassBuffers {
+    const unsigned int* cs;   // particle cell table (total_cells + 1)
+    const unsigned int* bcs;  // boundary cell table (total_cells + 1)
+    float4* pos4;
+    float4* vel4;
+    float4* aux4;
+    float4* flow4;
+    float4* adh4;
+    float4* avgadh4;
+    float4* drag4;
+    float4* acc4;
+    float4* col4;
+    float4* mat4;
+    const float4* bpos4;
+};
+
+void launchKeys(const LaunchCtx& c, const float4* pos4, unsigned int* keys);
+void launchBoundaryVolume(const LaunchCtx& c, int sid, int nb, float4* bpos4, const int* blabel,
+                          const unsigned int* bcs);
+void launchDensity(const LaunchCtx& c, const PassBuffers& b);
+void launchAvgFlow(const LaunchCtx& c, const PassBuffers& b);
+void launchVoidageAdhesion(const LaunchCtx& c, const PassBuffers& b);
+void launchSandMomentum(const LaunchCtx& c, const PassBuffers& b);
+void launchWaterMomentum(const LaunchCtx& c, const PassBuffers& b);
+void launchIntegrate(const LaunchCtx& c, const PassBuffers& b, float timeArg, int adaptive);
+
+// ---- stable LSD radix sort of 32-bit cell keys (sf_sort.cu) ----
+// Scratch sizes for sorting n keys.
+struct SortScratch {
+    unsigned int* keysAlt;   // n
+    unsigned int* vals;      // n
+    unsigned int* valsAlt;   // n
+    unsigned int* hist;      // 256 * tiles
+    int tiles;
+};
+int sortTiles(int n);
+// Sorts keys[0..n) (only the low `bits` bits are examined) and writes the
+// stable permutation to *permOut (new index -> old index) and the sorted keys
+// to *keysOut; both point into keys/scratch buffers. Returns kernels launched.
+int radixSort(cudaStream_t s, int n, int bits, unsigned int* keys, SortScratch& sc, unsigned int** keysOut,
+              unsigned int** permOut);
+// cellStart[c] = first index i with sortedKeys[i] >= c, for c in [0, nCells]
+void launchCellStart(cudaStream_t s, int n, int nCells, const unsigned int* sortedKeys, unsigned int* cellStart);
+// Gather the persistent per-slot arrays into sorted order.
+void launchReorder(cudaStream_t s, int n, const unsigned int* perm, const float4* pos, const float4* vel,
+                   const float4* col, const float4* mat, const float2* amc, const int* pid, float4* posOut,
+                   float4* velOut, float4* colOut, float4* matOut, float2* amcOut, int* pidOut);
+
+}  // namespace sfg

@@ -190,22 +190,41 @@ def tiny(seed: int = 7, sand=(10, 8, 10), water=(8, 12, 10)) -> Scene:
                        water_origin=(0.4 - 0.02 - (sand[0] - 1 + water[0]) * pitch, 0.02, 0.06))
 
 
-def _embankment_points(toe, crest, height, zs, pitch, y0):
-    """Lattice points of a trapezoid (1V:2H slopes) extruded along z."""
+def _axis(start, stop, pitch):
+    """Lattice coordinates start + k*pitch <= stop (k = 0, 1, ...)."""
+    if stop < start:
+        return np.zeros(0)
+    return start + pitch * np.arange(int(np.floor((stop - start) / pitch + 1e-9)) + 1)
+
+
+def _embankment_rows(toe, crest, height, pitch, y0):
+    """(y, x-coordinates) rows of a trapezoid with 1V:2H slopes on the floor."""
     base = crest + 4.0 * height
-    xs = np.arange(toe, toe + base + 1e-9, pitch)
-    ys = np.arange(y0, height + 1e-9, pitch)
-    X, Y, Z = np.meshgrid(xs, ys, zs, indexing="ij")
-    keep = (X >= toe + 2.0 * Y) & (X <= toe + base - 2.0 * Y)
-    return np.stack([X[keep], Y[keep], Z[keep]], 1)
+    xs = _axis(toe, toe + base, pitch)
+    rows = []
+    for y in _axis(y0, height, pitch):
+        rows.append((y, xs[(xs >= toe + 2.0 * y) & (xs <= toe + base - 2.0 * y)]))
+    return rows
 
 
-def _reservoir_points(x0, toe, level, zs, pitch, y0, gap):
-    xs = np.arange(x0, toe + 2.0 * level + 1e-9, pitch)
-    ys = np.arange(y0, level + 1e-9, pitch)
-    X, Y, Z = np.meshgrid(xs, ys, zs, indexing="ij")
-    keep = X < toe + 2.0 * Y - gap
-    return np.stack([X[keep], Y[keep], Z[keep]], 1)
+def _reservoir_rows(x0, toe, level, pitch, y0, gap):
+    """(y, x-coordinates) rows of water from x0 up to the upstream slope."""
+    xs = _axis(x0, toe + 2.0 * level, pitch)
+    return [(y, xs[xs < toe + 2.0 * y - gap]) for y in _axis(y0, level, pitch)]
+
+
+def _rows_count(rows, nz):
+    return sum(len(x) for _, x in rows) * nz
+
+
+def _rows_points(rows, zs):
+    pts = []
+    for y, xs in rows:
+        if len(xs) == 0:
+            continue
+        X, Z = np.meshgrid(xs, zs, indexing="ij")
+        pts.append(np.stack([X.ravel(), np.full(X.size, y), Z.ravel()], 1))
+    return np.concatenate(pts) if pts else np.zeros((0, 3))
 
 
 def plain_large(seed: int = 2024, target_sand: int = 500_000, target_water: int = 500_000) -> Scene:
@@ -217,39 +236,30 @@ def plain_large(seed: int = 2024, target_sand: int = 500_000, target_water: int 
     params = reference_params(sph_radius=r, dem_radius=r, dem_density=2650.0)
     bparams = boundary_params((0.0, 0.0, 0.0), box, params.sph_kernel_radius)
     rng = np.random.default_rng(seed)
-    zs_s = np.arange(2.0 * 2.0 * r, box[2] - 2.0 * r + 1e-9, pitch)     # z-min wall tests 2*rij
-    zs_w = np.arange(2.0 * r, box[2] - 2.0 * r + 1e-9, pitch)
+    zs_s = _axis(2.0 * 2.0 * r, box[2] - 2.0 * r, pitch)     # the z-min wall tests 2 * rij
+    zs_w = _axis(2.0 * r, box[2] - 2.0 * r, pitch)
     y0 = 2.0 * r
     height, level = 0.4, 0.35
-
-    def sand_for(crest, toe):
-        return _embankment_points(toe, crest, height, zs_s, pitch, y0)
-
-    # solve the reservoir length L (toe = x0 + L) for the water target
     x0 = 2.0 * r
-
-    def water_for(L):
-        return _reservoir_points(x0, x0 + L, level, zs_w, pitch, y0, gap=pitch)
-
     lo_L, hi_L = 0.1, 3.0
-    for _ in range(40):
+    for _ in range(50):
         mid = 0.5 * (lo_L + hi_L)
-        if water_for(mid).shape[0] < target_water:
+        if _rows_count(_reservoir_rows(x0, x0 + mid, level, pitch, y0, pitch), len(zs_w)) < target_water:
             lo_L = mid
         else:
             hi_L = mid
     L = hi_L
     toe = x0 + L
     lo_c, hi_c = 0.0, 2.0
-    for _ in range(40):
+    for _ in range(50):
         mid = 0.5 * (lo_c + hi_c)
-        if sand_for(mid, toe).shape[0] < target_sand:
+        if _rows_count(_embankment_rows(toe, mid, height, pitch, y0), len(zs_s)) < target_sand:
             lo_c = mid
         else:
             hi_c = mid
     crest = hi_c
-    sand = sand_for(crest, toe)
-    water = water_for(L)
+    sand = _rows_points(_embankment_rows(toe, crest, height, pitch, y0), zs_s)
+    water = _rows_points(_reservoir_rows(x0, toe, level, pitch, y0, pitch), zs_w)
     sand = (sand + rng.uniform(-0.01 * pitch, 0.01 * pitch, size=sand.shape)).astype(np.float32)
     water = (water + rng.uniform(-0.01 * pitch, 0.01 * pitch, size=water.shape)).astype(np.float32)
     meta = {"seed": seed, "crest": crest, "reservoir_length": L, "toe": toe,
