@@ -184,6 +184,8 @@ struct sf_handle {
     // per-substep arrays
     float4 *aux = nullptr, *flow = nullptr, *adh = nullptr, *avgadh = nullptr, *drag = nullptr, *acc = nullptr;
     unsigned int *keys = nullptr, *cs = nullptr, *bcs = nullptr;
+    int *nbrCnt = nullptr, *bnbrCnt = nullptr;
+    unsigned int *nbr = nullptr, *bnbr = nullptr;
     unsigned int* sortedKeys = nullptr;  // points into keys/scratch after a sort
     SortScratch sc{};
     float4* bpos = nullptr;
@@ -217,8 +219,20 @@ struct sf_handle {
     }
     PassBuffers buffers() const {
         PassBuffers b;
-        b.cs = cs;
-        b.bcs = bcs;
+        b.listsW.cnt = nbrCnt;
+        b.listsW.nbr = nbr;
+        b.listsW.bcnt = bnbrCnt;
+        b.listsW.bnbr = bnbr;
+        b.listsW.cs = cs;
+        b.listsW.bcs = bcs;
+        b.listsW.M = totalSlots;
+        b.lists.cnt = nbrCnt;
+        b.lists.nbr = nbr;
+        b.lists.bcnt = bnbrCnt;
+        b.lists.bnbr = bnbr;
+        b.lists.cs = cs;
+        b.lists.bcs = bcs;
+        b.lists.M = totalSlots;
         b.pos4 = pos[cur];
         b.vel4 = vel[cur];
         b.aux4 = aux;
@@ -250,12 +264,17 @@ struct sf_handle {
         devFree(drag);
         devFree(acc);
         devFree(keys);
+        devFree(nbrCnt);
+        devFree(bnbrCnt);
+        devFree(nbr);
+        devFree(bnbr);
         devFree(cs);
         devFree(bcs);
         devFree(sc.keysAlt);
         devFree(sc.vals);
         devFree(sc.valsAlt);
         devFree(sc.hist);
+        devFree(sc.digitTotal);
         devFree(bpos);
         devFree(blabel);
         devFree(dScenes);
@@ -444,11 +463,16 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
     SF_ALLOC(h->drag, F4);
     SF_ALLOC(h->acc, F4);
     SF_ALLOC(h->keys, sizeof(unsigned) * M);
+    SF_ALLOC(h->nbrCnt, sizeof(int) * M);
+    SF_ALLOC(h->bnbrCnt, sizeof(int) * M);
+    SF_ALLOC(h->nbr, sizeof(unsigned) * M * kMaxNbr);
+    SF_ALLOC(h->bnbr, sizeof(unsigned) * M * kMaxBNbr);
     SF_ALLOC(h->sc.keysAlt, sizeof(unsigned) * M);
     SF_ALLOC(h->sc.vals, sizeof(unsigned) * M);
     SF_ALLOC(h->sc.valsAlt, sizeof(unsigned) * M);
     h->sc.tiles = sortTiles(h->totalSlots);
     SF_ALLOC(h->sc.hist, sizeof(unsigned) * 256 * size_t(h->sc.tiles));
+    SF_ALLOC(h->sc.digitTotal, sizeof(unsigned) * 256);
     SF_ALLOC(h->cs, sizeof(unsigned) * (size_t(h->totalCells) + 1));
     SF_ALLOC(h->bcs, sizeof(unsigned) * (size_t(h->totalCells) + 1));
     SF_ALLOC(h->bpos, sizeof(float4) * std::max<size_t>(1, size_t(h->totalB)));
@@ -507,6 +531,8 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
         }
         hstate[s].n = int(in.n);
         hstate[s].n_sub = 1;
+        for (int64_t i = 0; i < in.nb; ++i)
+            if (in.blabel && in.blabel[i] == 1) h->hScenes[s].shape_boundary = 1;
     }
     hbcs[size_t(h->totalCells)] = unsigned(h->totalB);
     auto up = [&](void* d, const void* src, size_t bytes, const char* what) {
@@ -555,6 +581,7 @@ sf_status sf_set_params(sf_handle* h, int32_t scene, const sf_params* p) {
     S.cell_off = old.cell_off;
     S.b_off = old.b_off;
     S.nb = old.nb;
+    S.shape_boundary = old.shape_boundary;
     h->hScenes[scene] = S;
     return h->cuda(cudaMemcpyAsync(h->dScenes + scene, &S, sizeof(SceneDev), cudaMemcpyHostToDevice, h->stream),
                    "upload params");

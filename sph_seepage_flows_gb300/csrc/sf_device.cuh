@@ -63,6 +63,7 @@ struct SceneDev {
     BezierDev capG, adhG;
     float cd;
     int multi;
+    int shape_boundary;  // the scene has boundary particles with label 1
     float grav_abs;
     float gvx, gvy, gvz;
     float dry[3], wet[3];

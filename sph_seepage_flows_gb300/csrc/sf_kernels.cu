@@ -3,12 +3,22 @@
 // belongs to one scene (blockScene). Every pass is a gather: a thread writes
 // only its own slot, so no pass needs atomics except the per-scene max |acc|.
 //
-// The neighbor loops visit the 27 cells in the reference order
-// (m = 0..26, dx-major, e.g. cuda_sph_sf_solver_gpu.cuh:468-477) and, inside
-// a cell, run the reference's sub-loops in the reference order, so every
-// accumulator sums the same terms in the same order as the reference kernel.
-// Pairs farther apart than the interaction reach (all of whose terms are
-// exactly +0 in the reference) are skipped before any term is evaluated.
+// Neighbour lists. The density pass walks the reference's 27-cell stencil
+// (m = 0..26, dx-major, e.g. cuda_sph_sf_solver_gpu.cuh:468-477) once per
+// particle and records every particle (and every boundary particle) within
+// the interaction reach, in stencil order, into a column-major list
+// (entry k of slot i at k * M + i, so a warp reads 128 contiguous bytes per
+// entry). Pairs beyond the reach have all terms exactly +0 in the reference,
+// so the later passes iterate only the list: ~35 entries instead of ~216
+// stencil candidates per pass, with far less divergence between lanes. A
+// particle with more than kMaxNbr neighbours falls back to the stencil walk.
+//
+// Summation order. Density, average flow, voidage, saturation and adhesion
+// add their terms in exactly the reference order (list order = stencil
+// order), so they are bit-identical to the reference's FP32 arithmetic. The
+// two momentum passes evaluate all terms of a neighbour together instead of
+// one sub-loop per term and cell, which reorders their FP32 sums (rounding
+// differences ~1e-7 of the sum of term magnitudes).
 #include "sf_device.cuh"
 #include "sf_kernels.h"
 
@@ -42,6 +52,40 @@ __device__ __forceinline__ void forEachCell(const SceneDev& S, int3 c, F&& f) {
 }
 
 __device__ __forceinline__ bool inReach(const SceneDev& S, float3 d) { return dot3(d, d) < S.reach2; }
+
+// Particles within reach of slot, in stencil order (list, or stencil fallback).
+template <typename F>
+__device__ __forceinline__ void forFluidNeighbors(const SceneDev& S, const NbrLists& L, int slot, float3 pi,
+                                                  const float4* __restrict__ pos4, F&& f) {
+    const int c = L.cnt[slot];
+    if (c <= kMaxNbr) {
+        const unsigned* __restrict__ p = L.nbr + slot;
+#pragma unroll 1
+        for (int k = 0; k < c; ++k) f(int(p[size_t(k) * L.M]));
+    } else {
+        forEachCell(S, cellOf(S, pi), [&](int cell) {
+            for (unsigned j = L.cs[cell]; j < L.cs[cell + 1]; ++j)
+                if (inReach(S, pi - xyz(pos4[j]))) f(int(j));
+        });
+    }
+}
+
+// Boundary particles within reach of slot, in stencil order.
+template <typename F>
+__device__ __forceinline__ void forBoundaryNeighbors(const SceneDev& S, const NbrLists& L, int slot, float3 pi,
+                                                     const float4* __restrict__ bpos4, F&& f) {
+    const int c = L.bcnt[slot];
+    if (c <= kMaxBNbr) {
+        const unsigned* __restrict__ p = L.bnbr + slot;
+#pragma unroll 1
+        for (int k = 0; k < c; ++k) f(int(p[size_t(k) * L.M]));
+    } else {
+        forEachCell(S, cellOf(S, pi), [&](int cell) {
+            for (unsigned j = L.bcs[cell]; j < L.bcs[cell + 1]; ++j)
+                if (inReach(S, pi - xyz(bpos4[j]))) f(int(j));
+        });
+    }
+}
 
 // ---------------------------------------------------------------------- keys
 // Pos2GridHash (helper_thrust.cuh:66-89) into the global cell space; parking
@@ -79,39 +123,53 @@ __global__ void kBoundaryVolume(const SceneDev* __restrict__ scenes, int sid, fl
 }
 
 // ------------------------------------------------------------ density stage
-// ComputeSFDensity_CUDA + ComputeSFFluidDensity + ComputeBoundaryDensity
-// (cuda_sph_sf_solver_gpu.cuh:408-480, cuda_sph_solver_common_gpu.cuh:70-87)
+// Builds the neighbour lists and computes ComputeSFDensity_CUDA +
+// ComputeSFFluidDensity + ComputeBoundaryDensity (cuda_sph_sf_solver_gpu.cuh:
+// 408-480, cuda_sph_solver_common_gpu.cuh:70-87) in the same stencil walk,
 // fused with ComputeSFPressureByTait_CUDA (cuda_wcsph_sf_solver_gpu.cuh:19-44)
 // or ComputeSFPressure_CUDA (cuda_sph_sf_solver_gpu.cuh:482-508).
-__global__ void kDensity(const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene,
-                         SceneState* __restrict__ state, const unsigned int* __restrict__ cs,
-                         const unsigned int* __restrict__ bcs, const float4* __restrict__ pos4,
-                         const float4* __restrict__ bpos4, float4* __restrict__ vel4, float4* __restrict__ aux4) {
+__global__ void __launch_bounds__(kSlotAlign) kDensity(const SceneDev* __restrict__ scenes,
+                                                       const int* __restrict__ blockScene,
+                                                       SceneState* __restrict__ state, NbrListsW L,
+                                                       const float4* __restrict__ pos4,
+                                                       const float4* __restrict__ bpos4, float4* __restrict__ vel4,
+                                                       float4* __restrict__ aux4) {
     SF_SLOT_PROLOGUE
     if (slot == S.slot_off) state[sid].amax_bits = 0u;
     const float4 pi4 = pos4[slot];
     if (pi4.w == 0.f) return;
+    const float3 pi = xyz(pi4);
+    const bool water = pi4.w > 0.f;
+    float d = water ? pi4.w * S.W0 : 0.f;
+    int c = 0, bc = 0;
+    unsigned* __restrict__ nb = L.nbr + slot;
+    unsigned* __restrict__ bnb = L.bnbr + slot;
+    forEachCell(S, cellOf(S, pi), [&](int cell) {
+        const unsigned j1 = L.cs[cell + 1];
+        for (unsigned j = L.cs[cell]; j < j1; ++j) {
+            const float4 pj = pos4[j];
+            const float3 dij = pi - xyz(pj);
+            if (!inReach(S, dij)) continue;
+            if (c < kMaxNbr) nb[size_t(c) * L.M] = j;
+            ++c;
+            if (water && pj.w > 0.f) d += pj.w * poly6(S, len3(dij));  // label[i] == label[j]
+        }
+        const unsigned b1 = L.bcs[cell + 1];
+        for (unsigned j = L.bcs[cell]; j < b1; ++j) {
+            const float4 bj = bpos4[j];
+            const float3 dij = pi - xyz(bj);
+            if (!inReach(S, dij)) continue;
+            if (bc < kMaxBNbr) bnb[size_t(bc) * L.M] = j;
+            ++bc;
+            if (water) d += S.rho0 * fabsf(bj.w) * poly6(S, len3(dij));
+        }
+    });
+    L.cnt[slot] = c;
+    L.bcnt[slot] = bc;
     float density, pressure = 0.f;
-    if (pi4.w < 0.f) {
+    if (!water) {
         density = S.rho1;
     } else {
-        const float3 pi = xyz(pi4);
-        const float mi = pi4.w;
-        float d = mi * S.W0;
-        forEachCell(S, cellOf(S, pi), [&](int cell) {
-            for (unsigned j = cs[cell]; j < cs[cell + 1]; ++j) {
-                const float4 pj = pos4[j];
-                if (pj.w > 0.f) {  // label[i] == label[j] (water)
-                    const float3 dij = pi - xyz(pj);
-                    if (inReach(S, dij)) d += pj.w * poly6(S, len3(dij));
-                }
-            }
-            for (unsigned j = bcs[cell]; j < bcs[cell + 1]; ++j) {
-                const float4 bj = bpos4[j];
-                const float3 dij = pi - xyz(bj);
-                if (inReach(S, dij)) d += S.rho0 * fabsf(bj.w) * poly6(S, len3(dij));
-            }
-        });
         density = d;
         if (S.tait) {
             pressure = S.stiff * (powf(density / S.rho0, 7.f) - 1.f);
@@ -128,10 +186,12 @@ __global__ void kDensity(const SceneDev* __restrict__ scenes, const int* __restr
 // ------------------------------------------------------------ avg-flow stage
 // ComputeSFAvgFlow_CUDA with ComputeSFSandVolume and ComputeSFAvgFlow
 // (cuda_sph_sf_solver_gpu.cuh:111-173, 510-572). The two sub-loops feed
-// disjoint accumulators, so one sweep over the cell keeps every sum's order.
-__global__ void kAvgFlow(const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene,
-                         const unsigned int* __restrict__ cs, const float4* __restrict__ pos4,
-                         const float4* __restrict__ vel4, float4* __restrict__ aux4, float4* __restrict__ flow4) {
+// disjoint accumulators, so one sweep keeps every sum's reference order.
+__global__ void __launch_bounds__(kSlotAlign) kAvgFlow(const SceneDev* __restrict__ scenes,
+                                                       const int* __restrict__ blockScene, NbrLists L,
+                                                       const float4* __restrict__ pos4,
+                                                       const float4* __restrict__ vel4, float4* __restrict__ aux4,
+                                                       float4* __restrict__ flow4) {
     SF_SLOT_PROLOGUE
     const float4 pi4 = pos4[slot];
     if (pi4.w == 0.f) return;
@@ -139,24 +199,21 @@ __global__ void kAvgFlow(const SceneDev* __restrict__ scenes, const int* __restr
     const bool sandI = pi4.w < 0.f;
     float v_s = 0.f, v_w = 0.f, sand_volume = 0.f;
     float3 avg_s = mk3(0.f, 0.f, 0.f), avg_w = avg_s;
-    forEachCell(S, cellOf(S, pi), [&](int cell) {
-        for (unsigned j = cs[cell]; j < cs[cell + 1]; ++j) {
-            const float4 pj = pos4[j];
-            const float3 dij = pi - xyz(pj);
-            if (!inReach(S, dij)) continue;
-            const float4 vj4 = vel4[j];
-            const bool sandJ = pj.w < 0.f;
-            const float mj = fabsf(pj.w);
-            const float wij = poly6(S, len3(dij));
-            if (sandJ && vj4.w != 0.f) sand_volume += mj / vj4.w * wij;
-            const float vj = mj / vj4.w;
-            if (sandI && !sandJ) {
-                avg_s += xyz(vj4) * vj * wij;
-                v_s += vj * wij;
-            } else if (!sandI && sandJ) {
-                avg_w += xyz(vj4) * vj * wij;
-                v_w += vj * wij;
-            }
+    forFluidNeighbors(S, L, slot, pi, pos4, [&](int j) {
+        const float4 pj = pos4[j];
+        const float3 dij = pi - xyz(pj);
+        const float4 vj4 = vel4[j];
+        const bool sandJ = pj.w < 0.f;
+        const float mj = fabsf(pj.w);
+        const float wij = poly6(S, len3(dij));
+        if (sandJ && vj4.w != 0.f) sand_volume += mj / vj4.w * wij;
+        const float vj = mj / vj4.w;
+        if (sandI && !sandJ) {
+            avg_s += xyz(vj4) * vj * wij;
+            v_s += vj * wij;
+        } else if (!sandI && sandJ) {
+            avg_w += xyz(vj4) * vj * wij;
+            v_w += vj * wij;
         }
     });
     float3 avg;
@@ -178,12 +235,11 @@ __global__ void kAvgFlow(const SceneDev* __restrict__ scenes, const int* __restr
 // Sand: ComputeSFSandVoidage_CUDA (cuda_sph_sf_solver_gpu.cuh:209-238,
 // 680-721) and ComputeSFWetSandColor_CUDA (952-977). Water: the SF or MULTI
 // water adhesion kernel (175-207, 574-678). Reads the fluid voidage (aux.y)
-// of water neighbours and writes the final voidage (aux.w) of every slot.
-__global__ void kVoidageAdhesion(const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene,
-                                 const unsigned int* __restrict__ cs, const float4* __restrict__ pos4,
-                                 const float4* __restrict__ vel4, float4* __restrict__ aux4,
-                                 float4* __restrict__ adh4, float4* __restrict__ avgadh4,
-                                 float4* __restrict__ col4) {
+// of water neighbours and writes the final voidage (aux.w) of sand slots.
+__global__ void __launch_bounds__(kSlotAlign) kVoidageAdhesion(
+    const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene, NbrLists L,
+    const float4* __restrict__ pos4, const float4* __restrict__ vel4, float4* __restrict__ aux4,
+    float4* __restrict__ adh4, float4* __restrict__ avgadh4, float4* __restrict__ col4) {
     SF_SLOT_PROLOGUE
     const float4 pi4 = pos4[slot];
     if (pi4.w == 0.f) return;
@@ -191,17 +247,14 @@ __global__ void kVoidageAdhesion(const SceneDev* __restrict__ scenes, const int*
     if (pi4.w < 0.f) {
         const float sat = aux4[slot].z;
         float num = 0.f, den = 0.f;
-        forEachCell(S, cellOf(S, pi), [&](int cell) {
-            for (unsigned j = cs[cell]; j < cs[cell + 1]; ++j) {
-                const float4 pj = pos4[j];
-                if (!(pj.w > 0.f)) continue;
-                const float3 dij = pi - xyz(pj);
-                if (!inReach(S, dij)) continue;
-                const float vj = pj.w / vel4[j].w;
-                const float wij = poly6(S, len3(dij));
-                num += aux4[j].y * vj * wij;
-                den += vj * wij;
-            }
+        forFluidNeighbors(S, L, slot, pi, pos4, [&](int j) {
+            const float4 pj = pos4[j];
+            if (!(pj.w > 0.f)) return;
+            const float3 dij = pi - xyz(pj);
+            const float vj = pj.w / vel4[j].w;
+            const float wij = poly6(S, len3(dij));
+            num += aux4[j].y * vj * wij;
+            den += vj * wij;
         });
         aux4[slot].w = den != 0.f ? num / den : 0.f;
         // wet-sand colour ratchet
@@ -219,20 +272,17 @@ __global__ void kVoidageAdhesion(const SceneDev* __restrict__ scenes, const int*
         const float mi = pi4.w;
         float v_s = 0.f;
         float3 ad = mk3(0.f, 0.f, 0.f);
-        forEachCell(S, cellOf(S, pi), [&](int cell) {
-            for (unsigned j = cs[cell]; j < cs[cell + 1]; ++j) {
-                const float4 pj = pos4[j];
-                if (!(pj.w < 0.f)) continue;
-                const float3 dpij = pi - xyz(pj);
-                if (!inReach(S, dpij)) continue;
-                const float ldp = len3(dpij);
-                const float wij = poly6(S, ldp);
-                const float adij = adhesionSpline(S, ldp);
-                const float mj = -pj.w;
-                ad += bezier(S.adhG, aux4[j].z) * mi * mj * adij * dpij / fmaxf(kEps, ldp);
-                const float vj = mj / vel4[j].w;
-                v_s += vj * wij;
-            }
+        forFluidNeighbors(S, L, slot, pi, pos4, [&](int j) {
+            const float4 pj = pos4[j];
+            if (!(pj.w < 0.f)) return;
+            const float3 dpij = pi - xyz(pj);
+            const float ldp = len3(dpij);
+            const float wij = poly6(S, ldp);
+            const float adij = adhesionSpline(S, ldp);
+            const float mj = -pj.w;
+            ad += bezier(S.adhG, aux4[j].z) * mi * mj * adij * dpij / fmaxf(kEps, ldp);
+            const float vj = mj / vel4[j].w;
+            v_s += vj * wij;
         });
         adh4[slot] = make_float4(ad.x, ad.y, ad.z, 0.f);
         const float3 avg = v_s != 0.f ? ad / v_s : mk3(0.f, 0.f, 0.f);
@@ -241,17 +291,16 @@ __global__ void kVoidageAdhesion(const SceneDev* __restrict__ scenes, const int*
 }
 
 // ---------------------------------------------------------- sand momentum
-// Compute[Multi]SFSandLinearMomentum_CUDA (cuda_sph_sf_solver_gpu.cuh:723-897)
-// with the DEM, capillary, buoyancy, adhesion and boundary-DEM sub-loops per
-// cell (21-109, 240-273, 314-341) and ComputeDemWorldBoundaryForces
+// Compute[Multi]SFSandLinearMomentum_CUDA (cuda_sph_sf_solver_gpu.cuh:723-897):
+// DEM and capillary terms of sand neighbours (21-50, 83-109), buoyancy and
+// adhesion terms of water neighbours (240-273, 314-341), DEM against shape
+// boundary particles (52-81) and ComputeDemWorldBoundaryForces
 // (cuda_dem_solver_common_gpu.cuh:132-199). acc = g + 2 (f + df) / m.
-__global__ void kSandMomentum(const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene,
-                              const unsigned int* __restrict__ cs, const unsigned int* __restrict__ bcs,
-                              const float4* __restrict__ pos4, const float4* __restrict__ vel4,
-                              const float4* __restrict__ aux4, const float4* __restrict__ flow4,
-                              const float4* __restrict__ avgadh4, const float4* __restrict__ mat4,
-                              const float4* __restrict__ bpos4, float4* __restrict__ drag4,
-                              float4* __restrict__ acc4) {
+__global__ void __launch_bounds__(kSlotAlign) kSandMomentum(
+    const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene, NbrLists L,
+    const float4* __restrict__ pos4, const float4* __restrict__ vel4, const float4* __restrict__ aux4,
+    const float4* __restrict__ flow4, const float4* __restrict__ avgadh4, const float4* __restrict__ mat4,
+    const float4* __restrict__ bpos4, float4* __restrict__ drag4, float4* __restrict__ acc4) {
     SF_SLOT_PROLOGUE
     const float4 pi4 = pos4[slot];
     if (!(pi4.w < 0.f)) {
@@ -264,59 +313,34 @@ __global__ void kSandMomentum(const SceneDev* __restrict__ scenes, const int* __
     const float3 vi = xyz(vi4);
     const float di = vi4.w;
     const float4 ai = aux4[slot];
+    const float vol_i = mi / fmaxf(kEps, di);
     float v_w = 0.f;
     float3 f = mk3(0.f, 0.f, 0.f), df = f;
-    forEachCell(S, cellOf(S, pi), [&](int cell) {
-        const unsigned j0 = cs[cell], j1 = cs[cell + 1];
-        // ComputeSFUniRadiusDemForces (21-50)
-        for (unsigned j = j0; j < j1; ++j) {
-            const float4 pj = pos4[j];
-            if (!(pj.w < 0.f) || int(j) == slot) continue;
+    forFluidNeighbors(S, L, slot, pi, pos4, [&](int j) {
+        const float4 pj = pos4[j];
+        if (pj.w < 0.f) {
+            if (j == slot) return;
             const float3 dij = xyz(pj) - pi;
-            if (!inReach(S, dij)) continue;
             f += demForce(dij, xyz(vel4[j]) - vi, S.rij2, S.kn, S.ks, S.tan2);
-        }
-        // ComputeSFUniRadiusDemCapillaryForces (83-109)
-        for (unsigned j = j0; j < j1; ++j) {
-            const float4 pj = pos4[j];
-            if (!(pj.w < 0.f) || int(j) == slot) continue;
-            const float3 dij = xyz(pj) - pi;
-            if (!inReach(S, dij)) continue;
             f += capillaryForce(S, dij, (ai.z + aux4[j].z) / 2.f);
-        }
-        // ComputeSFSandBuoyancyForces (240-273)
-        for (unsigned j = j0; j < j1; ++j) {
-            const float4 pj = pos4[j];
-            if (!(pj.w > 0.f)) continue;
+        } else {
             const float3 dij = pi - xyz(pj);
-            if (!inReach(S, dij)) continue;
             const float4 aj = aux4[j];
-            if (!(aj.w > 0.f && aj.w <= 1.f)) continue;
-            const float dj = vel4[j].w / fmaxf(kEps, aj.w);
             const float wij = poly6(S, len3(dij));
-            const float3 nab = spikyGrad(S, dij);
-            v_w += pj.w / dj * wij;
-            f += -mi * pj.w * aj.x / fmaxf(kEps, di * dj) * nab;
-        }
-        // ComputeSFSandAdhesionTerm (314-341)
-        for (unsigned j = j0; j < j1; ++j) {
-            const float4 pj = pos4[j];
-            if (!(pj.w > 0.f)) continue;
-            const float3 dij = pi - xyz(pj);
-            if (!inReach(S, dij)) continue;
-            const float wij = poly6(S, len3(dij));
-            const float v = mi / fmaxf(kEps, di);
-            f += wij * v * xyz(avgadh4[j]);
-        }
-        // ComputeSFUniRadiusDemBoundaryForces (52-81): boundary particles with label 1
-        for (unsigned j = bcs[cell]; j < bcs[cell + 1]; ++j) {
-            const float4 bj = bpos4[j];
-            if (!(bj.w < 0.f)) continue;
-            const float3 dij = pi - xyz(bj);
-            if (!inReach(S, dij)) continue;
-            f += demForce(dij, mk3(-vi.x, -vi.y, -vi.z), S.rij2, S.kn, S.ks, S.tan2);
+            if (aj.w > 0.f && aj.w <= 1.f) {
+                const float dj = vel4[j].w / fmaxf(kEps, aj.w);
+                v_w += pj.w / dj * wij;
+                f += -mi * pj.w * aj.x / fmaxf(kEps, di * dj) * spikyGrad(S, dij);
+            }
+            f += wij * vol_i * xyz(avgadh4[j]);
         }
     });
+    if (S.shape_boundary) {
+        forBoundaryNeighbors(S, L, slot, pi, bpos4, [&](int b) {
+            const float4 bj = bpos4[b];
+            if (bj.w < 0.f) f += demForce(pi - xyz(bj), mk3(-vi.x, -vi.y, -vi.z), S.rij2, S.kn, S.ks, S.tan2);
+        });
+    }
     // ComputeDemWorldBoundaryForces; the z-min wall tests 2 * rij (DEM:191)
     {
         const float rij = S.wall_rij;
@@ -344,19 +368,17 @@ __global__ void kSandMomentum(const SceneDev* __restrict__ scenes, const int* __
 }
 
 // --------------------------------------------------------- water momentum
-// ComputeSFWaterLinearMomentum_CUDA (cuda_sph_sf_solver_gpu.cuh:899-950) with
-// the pressure (343-369), artificial viscosity (371-406), seepage (275-312),
-// boundary pressure and boundary viscosity (cuda_sph_solver_common_gpu.cuh:
-// 89-139; called with rho0 as the particle density) sub-loops per cell.
-// acc = g + (a - F_adh / m). Every thread then contributes |acc| of its slot
-// (sand included) to the scene maximum (cuda_wcsph_sf_solver.cu:43-47).
-__global__ void kWaterMomentum(const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene,
-                               SceneState* __restrict__ state, const unsigned int* __restrict__ cs,
-                               const unsigned int* __restrict__ bcs, const float4* __restrict__ pos4,
-                               const float4* __restrict__ vel4, const float4* __restrict__ aux4,
-                               const float4* __restrict__ drag4, const float4* __restrict__ adh4,
-                               const float4* __restrict__ bpos4, float4* __restrict__ acc4,
-                               unsigned int* errWord) {
+// ComputeSFWaterLinearMomentum_CUDA (cuda_sph_sf_solver_gpu.cuh:899-950):
+// pressure and artificial viscosity of water neighbours (343-406), seepage
+// terms of sand neighbours (275-312), boundary pressure and viscosity
+// (cuda_sph_solver_common_gpu.cuh:89-139, called with rho0 as the particle
+// density). acc = g + (a - F_adh / m). Every thread then contributes |acc|
+// of its slot (sand included) to the scene maximum (cuda_wcsph_sf_solver.cu:43-47).
+__global__ void __launch_bounds__(kSlotAlign) kWaterMomentum(
+    const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene, SceneState* __restrict__ state,
+    NbrLists L, const float4* __restrict__ pos4, const float4* __restrict__ vel4, const float4* __restrict__ aux4,
+    const float4* __restrict__ drag4, const float4* __restrict__ adh4, const float4* __restrict__ bpos4,
+    float4* __restrict__ acc4, unsigned int* errWord) {
     SF_SLOT_PROLOGUE
     const float4 pi4 = pos4[slot];
     float alen = 0.f;
@@ -369,39 +391,22 @@ __global__ void kWaterMomentum(const SceneDev* __restrict__ scenes, const int* _
         const float pri = ai4.x;
         const float pterm_i = pri / fmaxf(kEps, di * di);
         float3 a = mk3(0.f, 0.f, 0.f);
-        forEachCell(S, cellOf(S, pi), [&](int cell) {
-            const unsigned j0 = cs[cell], j1 = cs[cell + 1];
-            // ComputeSFWaterPressureTerm (343-369)
-            for (unsigned j = j0; j < j1; ++j) {
-                const float4 pj = pos4[j];
-                if (!(pj.w > 0.f) || int(j) == slot) continue;
-                const float3 dij = pi - xyz(pj);
-                if (!inReach(S, dij)) continue;
+        forFluidNeighbors(S, L, slot, pi, pos4, [&](int j) {
+            const float4 pj = pos4[j];
+            const float3 dij = pi - xyz(pj);
+            if (pj.w > 0.f) {
+                if (j == slot) return;
                 const float4 aj = aux4[j];
-                const float dj = vel4[j].w / fmaxf(kEps, aj.w);
-                a += -pj.w * (pterm_i + aj.x / fmaxf(kEps, dj * dj)) * spikyGrad(S, dij);
-            }
-            // ComputeSFWaterArtificialViscosity (371-406)
-            for (unsigned j = j0; j < j1; ++j) {
-                const float4 pj = pos4[j];
-                if (!(pj.w > 0.f) || int(j) == slot) continue;
-                const float3 dpij = pi - xyz(pj);
-                if (!inReach(S, dpij)) continue;
                 const float4 vj4 = vel4[j];
-                const float3 dv = vi - xyz(vj4);
-                const float dd = dot3(dv, dpij);
+                const float dj = vj4.w / fmaxf(kEps, aj.w);
+                const float3 nab = spikyGrad(S, dij);
+                a += -pj.w * (pterm_i + aj.x / fmaxf(kEps, dj * dj)) * nab;
+                const float dd = dot3(vi - xyz(vj4), dij);
                 if (dd < 0.f) {
-                    const float dj = vj4.w / fmaxf(kEps, aux4[j].w);
-                    const float pij = -S.nu / (di + dj) * (dd / (dot3(dpij, dpij) + kEps));
-                    a += -pj.w * pij * spikyGrad(S, dpij);
+                    const float pij = -S.nu / (di + dj) * (dd / (dot3(dij, dij) + kEps));
+                    a += -pj.w * pij * nab;
                 }
-            }
-            // ComputeSFWaterSeepageTerm (275-312)
-            for (unsigned j = j0; j < j1; ++j) {
-                const float4 pj = pos4[j];
-                if (!(pj.w < 0.f)) continue;
-                const float3 dij = pi - xyz(pj);
-                if (!inReach(S, dij)) continue;
+            } else {
                 const float dj = vel4[j].w;
                 const float wij = poly6(S, len3(dij));
                 const float3 nab = spikyGrad(S, dij);
@@ -409,23 +414,18 @@ __global__ void kWaterMomentum(const SceneDev* __restrict__ scenes, const int* _
                 const float3 drag = -wij / di * xyz(drag4[j]);
                 a += buoy + drag;
             }
-            // ComputeBoundaryPressure / ComputeBoundaryViscosity (rho0 as density)
-            const unsigned b0 = bcs[cell], b1 = bcs[cell + 1];
-            for (unsigned j = b0; j < b1; ++j) {
-                const float4 bj = bpos4[j];
-                const float3 dij = pi - xyz(bj);
-                if (!inReach(S, dij)) continue;
-                a += -S.rho0 * fabsf(bj.w) * (pri / fmaxf(kEps, S.rho0 * S.rho0)) * spikyGrad(S, dij);
-            }
-            for (unsigned j = b0; j < b1; ++j) {
-                const float4 bj = bpos4[j];
-                const float3 dpij = pi - xyz(bj);
-                if (!inReach(S, dpij)) continue;
-                const float dd = dot3(vi, dpij);
-                if (dd < 0.f) {
-                    const float pij = -S.bnu / (2.f * S.rho0) * (dd / (dot3(dpij, dpij) + kEps));
-                    a += -fabsf(bj.w) * S.rho0 * pij * spikyGrad(S, dpij);
-                }
+        });
+        const float bp = pri / fmaxf(kEps, S.rho0 * S.rho0);
+        const float bvis = -S.bnu / (2.f * S.rho0);
+        forBoundaryNeighbors(S, L, slot, pi, bpos4, [&](int b) {
+            const float4 bj = bpos4[b];
+            const float3 dij = pi - xyz(bj);
+            const float3 nab = spikyGrad(S, dij);
+            a += -S.rho0 * fabsf(bj.w) * bp * nab;
+            const float dd = dot3(vi, dij);
+            if (dd < 0.f) {
+                const float pij = bvis * (dd / (dot3(dij, dij) + kEps));
+                a += -fabsf(bj.w) * S.rho0 * pij * nab;
             }
         });
         const float3 g = mk3(0.f, 0.f, 0.f) + mk3(S.gvx, S.gvy, S.gvz);
@@ -509,19 +509,21 @@ __global__ void kIntegrate(const SceneDev* __restrict__ scenes, const int* __res
         if (tp.y < S.lpy + r2) { tp.y = S.lpy + r2; tv.y = fmaxf(tv.y, 0.f); }
         if (tp.z > S.hpz - r2) { tp.z = S.hpz - r2; tv.z = fminf(tv.z, 0.f); }
         if (tp.z < S.lpz + r2) { tp.z = S.lpz + r2; tv.z = fmaxf(tv.z, 0.f); }
-        forEachCell(S, cellOf(S, p), [&](int cell) {
-            for (unsigned j = bcs[cell]; j < bcs[cell + 1]; ++j) {
-                const float4 bj = bpos4[j];
-                if (!(bj.w < 0.f)) continue;
-                const float dpij = len3(p - xyz(bj));
-                const float overlap = dpij - r2;
-                if (overlap < 0.f) {
-                    const float3 nn = (p - xyz(bj)) / dpij;
-                    tv = tv * 0.f;
-                    tp += nn * -overlap;
+        if (S.shape_boundary) {  // only boundary particles with label 1 push water out
+            forEachCell(S, cellOf(S, p), [&](int cell) {
+                for (unsigned j = bcs[cell]; j < bcs[cell + 1]; ++j) {
+                    const float4 bj = bpos4[j];
+                    if (!(bj.w < 0.f)) continue;
+                    const float dpij = len3(p - xyz(bj));
+                    const float overlap = dpij - r2;
+                    if (overlap < 0.f) {
+                        const float3 nn = (p - xyz(bj)) / dpij;
+                        tv = tv * 0.f;
+                        tp += nn * -overlap;
+                    }
                 }
-            }
-        });
+            });
+        }
         p = tp;
         v = tv;
     }
@@ -544,35 +546,35 @@ void launchBoundaryVolume(const LaunchCtx& c, int sid, int nb, float4* bpos4, co
 }
 
 void launchDensity(const LaunchCtx& c, const PassBuffers& b) {
-    kDensity<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, c.state, b.cs, b.bcs, b.pos4,
-                                                        b.bpos4, b.vel4, b.aux4);
+    kDensity<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, c.state, b.listsW, b.pos4, b.bpos4,
+                                                        b.vel4, b.aux4);
 }
 
 void launchAvgFlow(const LaunchCtx& c, const PassBuffers& b) {
-    kAvgFlow<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, b.cs, b.pos4, b.vel4, b.aux4,
+    kAvgFlow<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, b.lists, b.pos4, b.vel4, b.aux4,
                                                         b.flow4);
 }
 
 void launchVoidageAdhesion(const LaunchCtx& c, const PassBuffers& b) {
-    kVoidageAdhesion<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, b.cs, b.pos4, b.vel4,
+    kVoidageAdhesion<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, b.lists, b.pos4, b.vel4,
                                                                 b.aux4, b.adh4, b.avgadh4, b.col4);
 }
 
 void launchSandMomentum(const LaunchCtx& c, const PassBuffers& b) {
-    kSandMomentum<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, b.cs, b.bcs, b.pos4, b.vel4,
+    kSandMomentum<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, b.lists, b.pos4, b.vel4,
                                                              b.aux4, b.flow4, b.avgadh4, b.mat4, b.bpos4, b.drag4,
                                                              b.acc4);
 }
 
 void launchWaterMomentum(const LaunchCtx& c, const PassBuffers& b) {
-    kWaterMomentum<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, c.state, b.cs, b.bcs,
-                                                              b.pos4, b.vel4, b.aux4, b.drag4, b.adh4, b.bpos4,
-                                                              b.acc4, c.errWord);
+    kWaterMomentum<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, c.state, b.lists, b.pos4,
+                                                              b.vel4, b.aux4, b.drag4, b.adh4, b.bpos4, b.acc4,
+                                                              c.errWord);
 }
 
 void launchIntegrate(const LaunchCtx& c, const PassBuffers& b, float timeArg, int adaptive) {
     kIntegrate<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, c.state, timeArg, adaptive,
-                                                          b.bcs, b.bpos4, b.pos4, b.vel4, b.acc4, b.adh4,
+                                                          b.lists.bcs, b.bpos4, b.pos4, b.vel4, b.acc4, b.adh4,
                                                           b.avgadh4);
 }
 

@@ -19,10 +19,33 @@ struct LaunchCtx {
     int slotBlocks;           // total slots / kSlotAlign
 };
 
-// Device buffers the neighbor passes read and write (current sort order).
-struct PassBuffers {
+// Neighbour lists of the current substep (column-major: entry k of slot i at
+// k * M + i). A count above the capacity means "walk the stencil instead".
+constexpr int kMaxNbr = 64;
+constexpr int kMaxBNbr = 48;
+struct NbrLists {
+    const int* cnt;
+    const unsigned int* nbr;
+    const int* bcnt;
+    const unsigned int* bnbr;
     const unsigned int* cs;   // particle cell table (total_cells + 1)
     const unsigned int* bcs;  // boundary cell table (total_cells + 1)
+    long long M;              // total slots
+};
+struct NbrListsW {
+    int* cnt;
+    unsigned int* nbr;
+    int* bcnt;
+    unsigned int* bnbr;
+    const unsigned int* cs;
+    const unsigned int* bcs;
+    long long M;
+};
+
+// Device buffers the neighbor passes read and write (current sort order).
+struct PassBuffers {
+    NbrLists lists;
+    NbrListsW listsW;
     float4* pos4;
     float4* vel4;
     float4* aux4;
@@ -53,6 +76,7 @@ struct SortScratch {
     unsigned int* vals;      // n
     unsigned int* valsAlt;   // n
     unsigned int* hist;      // 256 * tiles
+    unsigned int* digitTotal;  // 256
     int tiles;
 };
 int sortTiles(int n);

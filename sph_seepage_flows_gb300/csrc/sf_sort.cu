@@ -9,8 +9,8 @@
 // cellStart[c] is the lower bound of c in the sorted keys. The result is the
 // same permutation and the same table as the reference's.
 //
-// Per 8-bit digit pass: kHist (per-tile digit counts), kScan (one block,
-// digit-major exclusive scan over tiles) and kScatter (in-tile stable rank:
+// Per 8-bit digit pass: kHist (per-tile digit counts), kScanTiles (per digit,
+// exclusive scan over tiles) and kScatter (digit offsets, in-tile stable rank:
 // rounds of 256 keys in index order, warp match for the rank inside a warp,
 // shared per-warp digit counts for the rank across warps).
 #include "sf_kernels.h"
@@ -20,7 +20,6 @@ namespace sfg {
 constexpr int kSortThreads = 256;
 constexpr int kSortItems = 16;
 constexpr int kTile = kSortThreads * kSortItems;
-constexpr int kScanThreads = 1024;
 
 int sortTiles(int n) { return (n + kTile - 1) / kTile; }
 
@@ -39,41 +38,54 @@ __global__ void __launch_bounds__(kSortThreads) kHist(const unsigned int* __rest
     hist[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
 }
 
-// In-place exclusive scan of hist[0..len) by one block.
-__global__ void __launch_bounds__(kScanThreads) kScan(unsigned int* __restrict__ hist, int len) {
-    __shared__ unsigned int part[kScanThreads];
-    const int chunk = (len + kScanThreads - 1) / kScanThreads;
-    const int b = threadIdx.x * chunk;
-    const int e = min(b + chunk, len);
-    unsigned int s = 0;
-    for (int i = b; i < e; ++i) s += hist[i];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = 1; o < kScanThreads; o <<= 1) {
-        unsigned int v = threadIdx.x >= o ? part[threadIdx.x - o] : 0u;
+// Per-digit exclusive scan over tiles: block d scans hist[d * tiles ..
+// d * tiles + tiles) in place and writes the digit's total.
+__global__ void __launch_bounds__(kSortThreads) kScanTiles(unsigned int* __restrict__ hist, int tiles,
+                                                           unsigned int* __restrict__ digitTotal) {
+    __shared__ unsigned int part[kSortThreads];
+    unsigned int* h = hist + size_t(blockIdx.x) * tiles;
+    unsigned int carry = 0;
+    for (int base = 0; base < tiles; base += kSortThreads) {
+        const int t = base + threadIdx.x;
+        const unsigned int v = t < tiles ? h[t] : 0u;
+        part[threadIdx.x] = v;
         __syncthreads();
-        part[threadIdx.x] += v;
+        for (int o = 1; o < kSortThreads; o <<= 1) {
+            const unsigned int u = threadIdx.x >= o ? part[threadIdx.x - o] : 0u;
+            __syncthreads();
+            part[threadIdx.x] += u;
+            __syncthreads();
+        }
+        if (t < tiles) h[t] = carry + part[threadIdx.x] - v;
+        carry += part[kSortThreads - 1];
         __syncthreads();
     }
-    unsigned int run = part[threadIdx.x] - s;
-    for (int i = b; i < e; ++i) {
-        const unsigned int v = hist[i];
-        hist[i] = run;
-        run += v;
-    }
+    if (threadIdx.x == 0) digitTotal[blockIdx.x] = carry;
 }
 
 __global__ void __launch_bounds__(kSortThreads) kScatter(const unsigned int* __restrict__ keysIn,
                                                          const unsigned int* __restrict__ valsIn,
                                                          unsigned int* __restrict__ keysOut,
                                                          unsigned int* __restrict__ valsOut, int n, int shift,
-                                                         const unsigned int* __restrict__ hist, int tiles) {
+                                                         const unsigned int* __restrict__ hist, int tiles,
+                                                         const unsigned int* __restrict__ digitTotal) {
     constexpr int kWarps = kSortThreads / 32;
     __shared__ unsigned int base[256];
     __shared__ unsigned int running[256];
     __shared__ unsigned int cnt[kWarps][256];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    base[tid] = hist[tid * tiles + blockIdx.x];
+    // digit offsets: exclusive scan of the digit totals
+    const unsigned int tot0 = digitTotal[tid];
+    running[tid] = tot0;
+    __syncthreads();
+    for (int o = 1; o < 256; o <<= 1) {
+        const unsigned int u = tid >= o ? running[tid - o] : 0u;
+        __syncthreads();
+        running[tid] += u;
+        __syncthreads();
+    }
+    base[tid] = running[tid] - tot0 + hist[tid * tiles + blockIdx.x];
+    __syncthreads();
     running[tid] = 0;
 #pragma unroll
     for (int w = 0; w < kWarps; ++w) cnt[w][tid] = 0;
@@ -124,8 +136,8 @@ int radixSort(cudaStream_t s, int n, int bits, unsigned int* keys, SortScratch& 
     for (int p = 0; p < passes; ++p) {
         const int shift = 8 * p;
         kHist<<<tiles, kSortThreads, 0, s>>>(kIn, n, shift, sc.hist, tiles);
-        kScan<<<1, kScanThreads, 0, s>>>(sc.hist, 256 * tiles);
-        kScatter<<<tiles, kSortThreads, 0, s>>>(kIn, vIn, kOut, vOut, n, shift, sc.hist, tiles);
+        kScanTiles<<<256, kSortThreads, 0, s>>>(sc.hist, tiles, sc.digitTotal);
+        kScatter<<<tiles, kSortThreads, 0, s>>>(kIn, vIn, kOut, vOut, n, shift, sc.hist, tiles, sc.digitTotal);
         launches += 3;
         // next pass reads what this one wrote
         unsigned int* t = kIn;
