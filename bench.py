@@ -143,6 +143,48 @@ def cpu_baseline(sc, dt, budget_s=20.0):
                       f"(FP32 CPU restatement of the reference kernels, OpenMP)"}
 
 
+def batched_comparison(stream, substeps=100, n_scenes=64, blocks=2):
+    """The batched-ensemble workload: n_scenes independent scenes (log-uniform
+    2k-60k particles, per-scene friction/capillary/permeability) advanced in
+    the same launches by one handle, against a loop over one handle per scene
+    on the same GPU. Both replay captured graphs of `substeps`-substep blocks
+    (graph capture covers two substeps; a block is substeps/2 replays)."""
+    import torch
+
+    from sph_seepage_flows_gb300 import capi, scenes
+    sc = scenes.batched(n_scenes=n_scenes)
+    dt = reference_dt(sc[0])
+    total = sum(s.n for s in sc)
+    batch = capi.Simulation(sc, stream=stream.cuda_stream)
+    singles = [capi.Simulation(s, stream=stream.cuda_stream) for s in sc]
+    batch.substeps_fixed(dt, 4)
+    for s in singles:
+        s.substeps_fixed(dt, 4)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(blocks):
+        batch.substeps_fixed(dt, substeps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_batch = e0.elapsed_time(e1) / 1e3
+    e0.record(stream)
+    for _ in range(blocks):
+        for s in singles:
+            s.substeps_fixed(dt, substeps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_loop = e0.elapsed_time(e1) / 1e3
+    flags = batch.check_error()
+    for s in singles:
+        flags |= s.check_error()
+    v_batch = total * substeps * blocks / t_batch
+    v_loop = total * substeps * blocks / t_loop
+    return {"scenes": n_scenes, "particles": total, "substeps": substeps * blocks, "dt": dt,
+            "batched_value": v_batch, "per_scene_loop_value": v_loop, "speedup": v_batch / v_loop,
+            "unit": "particle-substeps/s", "device_error_flags": flags}
+
+
 def run_reference(args, rank, world):
     """--impl reference: the reference kernels' FP32 CPU restatement."""
     if rank != 0:
@@ -266,6 +308,14 @@ def run_ours(args, rank, world):
                "path": "sf_set_field(pos, vel; pinned host) + sf_substeps_fixed(1) + sf_get_field(pos, vel)"}
 
     flags = sim.check_error()
+    # pair interactions per substep: for every particle, the particles within
+    # the interaction reach (itself excluded) times the neighbour passes it
+    # takes part in (water: density, avg flow, adhesion, momentum; sand: avg
+    # flow, voidage, momentum)
+    nbrs = sim.field("neighbors").astype(np.int64) - 1
+    lab = sim.field("label")
+    pairs = int(4 * nbrs[lab == 0].sum() + 3 * nbrs[lab == 1].sum())
+    batched = None if args.no_batched else batched_comparison(stream)
     if rank != 0:
         return
     cpu = None if args.no_cpu else cpu_baseline(sc, dt)
@@ -283,11 +333,15 @@ def run_ours(args, rank, world):
                      "algorithmic_bytes_per_particle": STAGE_BYTES[top]},
         "substep_roofline_frac": BYTES_PER_SUBSTEP * n / (ms / steps * 1e-3) / 1e9 / peak,
         "stage_ms": stage_ms,
+        "pairs_per_substep": pairs,
+        "pair_interactions_per_s": world * pairs * steps / (ms * 1e-3),
+        "mean_neighbors": float(nbrs.mean()),
         "gpu_launches": launches,
         "device_error_flags": flags,
         "clocks": clk,
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "batched": batched,
     }
     print(json.dumps(line), flush=True)
 
@@ -301,6 +355,7 @@ def main():
     ap.add_argument("--workload", default="plain_large")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

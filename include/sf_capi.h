@@ -133,7 +133,9 @@ enum {
     SF_FIELD_AMCAMCP = 17,       /* f32 x2 */
     SF_FIELD_ID = 18,            /* i32: creation index of the particle */
     SF_FIELD_KEY = 19,           /* i32: scene-local cell key of the last sort */
-    SF_FIELD_COUNT = 20,
+    SF_FIELD_NEIGHBORS = 20,     /* i32: particles within the interaction reach at the last
+                                    density pass, the particle itself included */
+    SF_FIELD_COUNT = 21,
     SF_BFIELD_POS = 32,          /* f32 x3, boundary particles in sorted order */
     SF_BFIELD_LABEL = 33,        /* i32 */
     SF_BFIELD_VOLUME = 34        /* f32 (Akinci volume) */

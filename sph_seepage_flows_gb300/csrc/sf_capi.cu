@@ -105,8 +105,10 @@ SceneDev makeSceneDev(const sf_params& P, const sf_boundary_params& B, const sf_
         S.cap_cos = cosf(contact_angle);
         S.cap_sin = sinf(contact_angle);
         S.cap_m2pi = -2.f * kPiF;
-        double reach = std::max(double(h), double(2.f * r) + double(s_rupture));
+        double demReach = double(2.f * r) + double(s_rupture);
+        double reach = std::max(double(h), demReach);
         S.reach2 = float(reach * reach * (1.0 + 1e-5));
+        S.dem_reach2 = float(demReach * demReach * (1.0 + 1e-5));
     }
     S.capG = makeBezier(P.sf_c0, P.sf_cmc, P.sf_cmc_p, P.sf_csat);
     S.multi = P.sf_type == SF_TYPE_MULTI_SF ? 1 : 0;
@@ -184,7 +186,8 @@ struct sf_handle {
     // per-substep arrays
     float4 *aux = nullptr, *flow = nullptr, *adh = nullptr, *avgadh = nullptr, *drag = nullptr, *acc = nullptr;
     unsigned int *keys = nullptr, *cs = nullptr, *bcs = nullptr;
-    int *nbrCnt = nullptr, *bnbrCnt = nullptr;
+    unsigned int* nbrCnt = nullptr;
+    int* bnbrCnt = nullptr;
     unsigned int *nbr = nullptr, *bnbr = nullptr;
     unsigned int* sortedKeys = nullptr;  // points into keys/scratch after a sort
     SortScratch sc{};
@@ -463,7 +466,7 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
     SF_ALLOC(h->drag, F4);
     SF_ALLOC(h->acc, F4);
     SF_ALLOC(h->keys, sizeof(unsigned) * M);
-    SF_ALLOC(h->nbrCnt, sizeof(int) * M);
+    SF_ALLOC(h->nbrCnt, sizeof(unsigned) * M);
     SF_ALLOC(h->bnbrCnt, sizeof(int) * M);
     SF_ALLOC(h->nbr, sizeof(unsigned) * M * kMaxNbr);
     SF_ALLOC(h->bnbr, sizeof(unsigned) * M * kMaxBNbr);
@@ -701,7 +704,7 @@ __global__ void kGetField(int field, int n, int slotOff, int cellOff, int order,
                           const int* __restrict__ pid, const float4* __restrict__ aux, const float4* __restrict__ flow,
                           const float4* __restrict__ adh, const float4* __restrict__ avgadh,
                           const float4* __restrict__ drag, const float4* __restrict__ acc,
-                          const unsigned int* __restrict__ keys, void* out) {
+                          const unsigned int* __restrict__ keys, const unsigned int* __restrict__ cnt, void* out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int s = slotOff + i;
@@ -737,6 +740,7 @@ __global__ void kGetField(int field, int n, int slotOff, int cellOff, int order,
         break;
     case SF_FIELD_ID: iv[o] = pid[s]; break;
     case SF_FIELD_KEY: iv[o] = keys ? int(keys[s]) - cellOff : -1; break;
+    case SF_FIELD_NEIGHBORS: iv[o] = cnt ? int(cnt[s] & 0xFFFFu) + int(cnt[s] >> 16) : 0; break;
     default: break;
     }
 }
@@ -793,7 +797,7 @@ int fieldWidth(int field) {
     case SF_FIELD_AMCAMCP: return 2;
     case SF_FIELD_LABEL: case SF_FIELD_RADIUS: case SF_FIELD_MASS: case SF_FIELD_DENSITY: case SF_FIELD_PRESSURE:
     case SF_FIELD_VOIDAGE: case SF_FIELD_SATURATION: case SF_FIELD_MAX_SATURATION: case SF_FIELD_ID:
-    case SF_FIELD_KEY: case SF_BFIELD_LABEL: case SF_BFIELD_VOLUME:
+    case SF_FIELD_KEY: case SF_FIELD_NEIGHBORS: case SF_BFIELD_LABEL: case SF_BFIELD_VOLUME:
         return 1;
     default: return 0;
     }
@@ -853,7 +857,7 @@ sf_status sf_get_field(sf_handle* h, int32_t scene, int32_t field, int32_t order
         kGetField<<<blocks, 256, 0, h->stream>>>(field, int(n), S.slot_off, S.cell_off, order, h->pos[c], h->vel[c],
                                                  h->col[c], h->mat[c], h->amc[c], h->pid[c], h->aux, h->flow,
                                                  h->adh, h->avgadh, h->drag, h->acc, h->sorted ? h->sortedKeys : nullptr,
-                                                 target);
+                                                 h->sorted ? h->nbrCnt : nullptr, target);
     }
     if (h->cuda(cudaGetLastError(), "get_field launch")) return SF_ERR_CUDA;
     if (!dst_on_device) {
@@ -868,7 +872,8 @@ sf_status sf_set_field(sf_handle* h, int32_t scene, int32_t field, int32_t order
                        int32_t src_on_device) {
     if (!h || !src || scene < 0 || scene >= h->nScenes) return SF_ERR_INVALID;
     const int w = fieldWidth(field);
-    if (w == 0 || field >= SF_BFIELD_POS || field == SF_FIELD_ID || field == SF_FIELD_KEY)
+    if (w == 0 || field >= SF_BFIELD_POS || field == SF_FIELD_ID || field == SF_FIELD_KEY ||
+        field == SF_FIELD_NEIGHBORS)
         return h->fail(SF_ERR_INVALID, "field cannot be set");
     if (order != SF_ORDER_SORTED && order != SF_ORDER_ID) return h->fail(SF_ERR_INVALID, "unknown order");
     const SceneDev& S = h->hScenes[scene];

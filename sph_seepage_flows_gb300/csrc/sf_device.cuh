@@ -57,7 +57,8 @@ struct SceneDev {
     int tait;
     // sand
     float rho1, dem_radius, kn, ks, tan2, damping, wall_rij;
-    float rij2;  // 2 * dem_radius
+    float rij2;       // 2 * dem_radius
+    float dem_reach2; // (2 * dem_radius + rupture distance)^2, widened: DEM and capillary vanish beyond
     // capillary bridge constants (cuda_dem_solver_common_gpu.cuh:53-90)
     float cap_vlb, cap_srupt, cap_vlb_pir, cap_pir, cap_cos, cap_sin, cap_m2pi;
     BezierDev capG, adhG;

@@ -6,19 +6,28 @@
 // Neighbour lists. The density pass walks the reference's 27-cell stencil
 // (m = 0..26, dx-major, e.g. cuda_sph_sf_solver_gpu.cuh:468-477) once per
 // particle and records every particle (and every boundary particle) within
-// the interaction reach, in stencil order, into a column-major list
-// (entry k of slot i at k * M + i, so a warp reads 128 contiguous bytes per
-// entry). Pairs beyond the reach have all terms exactly +0 in the reference,
-// so the later passes iterate only the list: ~35 entries instead of ~216
-// stencil candidates per pass, with far less divergence between lanes. A
-// particle with more than kMaxNbr neighbours falls back to the stencil walk.
+// the interaction reach into a column-major list (entry k of slot i at
+// k * M + i, so a warp reads 128 contiguous bytes per entry): sand
+// neighbours from the front, water neighbours from the back, each in stencil
+// order. Pairs beyond the reach have all terms exactly +0 in the reference,
+// so the later passes iterate only the list (~35 entries instead of ~216
+// stencil candidates), one label class at a time (no label divergence). A
+// particle whose list overflows falls back to the stencil walk.
 //
-// Summation order. Density, average flow, voidage, saturation and adhesion
-// add their terms in exactly the reference order (list order = stencil
-// order), so they are bit-identical to the reference's FP32 arithmetic. The
-// two momentum passes evaluate all terms of a neighbour together instead of
-// one sub-loop per term and cell, which reorders their FP32 sums (rounding
-// differences ~1e-7 of the sum of term magnitudes).
+// The walk itself is warp-cooperative when the warp's particles share one
+// cell column: the warp streams the union of its members' z-windows through
+// shared memory once per column, each lane keeping the candidates of its own
+// window, so every lane sees its candidates in stencil order.
+//
+// Summation order. Every accumulator of the density, average-flow, voidage,
+// saturation and adhesion passes receives one label class of neighbours, in
+// stencil order, exactly as in the reference kernel, so those fields are
+// bit-identical to the reference's FP32 arithmetic (density near walls is
+// recomputed with the reference's fluid/boundary interleaving per cell). The
+// two momentum passes evaluate all terms of a neighbour together, sand
+// neighbours before water neighbours, instead of one sub-loop per term and
+// cell, which reorders their FP32 sums (differences ~1e-7 of the sum of term
+// magnitudes).
 #include "sf_device.cuh"
 #include "sf_kernels.h"
 
@@ -53,21 +62,37 @@ __device__ __forceinline__ void forEachCell(const SceneDev& S, int3 c, F&& f) {
 
 __device__ __forceinline__ bool inReach(const SceneDev& S, float3 d) { return dot3(d, d) < S.reach2; }
 
-// Particles within reach of slot, in stencil order (list, or stencil fallback).
-template <typename F>
-__device__ __forceinline__ void forFluidNeighbors(const SceneDev& S, const NbrLists& L, int slot, float3 pi,
+// Neighbours of one label within reach of slot, in stencil order: the sand
+// part (kSand) or the water part of the list, or the stencil when the list
+// overflowed.
+template <bool kSand, typename F>
+__device__ __forceinline__ void forLabelNeighbors(const SceneDev& S, const NbrLists& L, int slot, float3 pi,
                                                   const float4* __restrict__ pos4, F&& f) {
-    const int c = L.cnt[slot];
-    if (c <= kMaxNbr) {
-        const unsigned* __restrict__ p = L.nbr + slot;
-#pragma unroll 1
-        for (int k = 0; k < c; ++k) f(int(p[size_t(k) * L.M]));
+    const unsigned c = L.cnt[slot];
+    if (int(c & 0xFFFFu) + int(c >> 16) <= kMaxNbr) {
+        const int n = kSand ? int(c & 0xFFFFu) : int(c >> 16);
+        const unsigned* __restrict__ p = L.nbr + slot + (kSand ? 0 : size_t(kMaxNbr - 1) * L.M);
+        const long long step = kSand ? L.M : -L.M;
+#pragma unroll 2
+        for (int k = 0; k < n; ++k) f(int(p[k * step]));
     } else {
         forEachCell(S, cellOf(S, pi), [&](int cell) {
-            for (unsigned j = L.cs[cell]; j < L.cs[cell + 1]; ++j)
-                if (inReach(S, pi - xyz(pos4[j]))) f(int(j));
+            for (unsigned j = L.cs[cell]; j < L.cs[cell + 1]; ++j) {
+                const float4 pj = pos4[j];
+                if ((kSand ? pj.w < 0.f : pj.w > 0.f) && inReach(S, pi - xyz(pj))) f(int(j));
+            }
         });
     }
+}
+template <typename F>
+__device__ __forceinline__ void forSandNeighbors(const SceneDev& S, const NbrLists& L, int slot, float3 pi,
+                                                 const float4* __restrict__ pos4, F&& f) {
+    forLabelNeighbors<true>(S, L, slot, pi, pos4, f);
+}
+template <typename F>
+__device__ __forceinline__ void forWaterNeighbors(const SceneDev& S, const NbrLists& L, int slot, float3 pi,
+                                                  const float4* __restrict__ pos4, F&& f) {
+    forLabelNeighbors<false>(S, L, slot, pi, pos4, f);
 }
 
 // Boundary particles within reach of slot, in stencil order.
@@ -123,11 +148,34 @@ __global__ void kBoundaryVolume(const SceneDev* __restrict__ scenes, int sid, fl
 }
 
 // ------------------------------------------------------------ density stage
-// Builds the neighbour lists and computes ComputeSFDensity_CUDA +
-// ComputeSFFluidDensity + ComputeBoundaryDensity (cuda_sph_sf_solver_gpu.cuh:
-// 408-480, cuda_sph_solver_common_gpu.cuh:70-87) in the same stencil walk,
-// fused with ComputeSFPressureByTait_CUDA (cuda_wcsph_sf_solver_gpu.cuh:19-44)
-// or ComputeSFPressure_CUDA (cuda_sph_sf_solver_gpu.cuh:482-508).
+// Water density of ComputeSFDensity_CUDA + ComputeSFFluidDensity +
+// ComputeBoundaryDensity (cuda_sph_sf_solver_gpu.cuh:408-480,
+// cuda_sph_solver_common_gpu.cuh:70-87): m_i W(0) plus, cell by cell of the
+// stencil, the water particles of the cell then the boundary particles of
+// the cell.
+__device__ __forceinline__ float exactDensity(const SceneDev& S, const NbrListsW& L, float3 pi, float mi,
+                                              const float4* __restrict__ pos4, const float4* __restrict__ bpos4) {
+    float d = mi * S.W0;
+    forEachCell(S, cellOf(S, pi), [&](int cell) {
+        for (unsigned j = L.cs[cell]; j < L.cs[cell + 1]; ++j) {
+            const float4 pj = pos4[j];
+            if (pj.w > 0.f) {
+                const float3 dij = pi - xyz(pj);
+                if (inReach(S, dij)) d += pj.w * poly6(S, len3(dij));
+            }
+        }
+        for (unsigned j = L.bcs[cell]; j < L.bcs[cell + 1]; ++j) {
+            const float4 bj = bpos4[j];
+            const float3 dij = pi - xyz(bj);
+            if (inReach(S, dij)) d += S.rho0 * fabsf(bj.w) * poly6(S, len3(dij));
+        }
+    });
+    return d;
+}
+
+// Builds the neighbour lists and computes the density, fused with
+// ComputeSFPressureByTait_CUDA (cuda_wcsph_sf_solver_gpu.cuh:19-44) or
+// ComputeSFPressure_CUDA (cuda_sph_sf_solver_gpu.cuh:482-508).
 __global__ void __launch_bounds__(kSlotAlign) kDensity(const SceneDev* __restrict__ scenes,
                                                        const int* __restrict__ blockScene,
                                                        SceneState* __restrict__ state, NbrListsW L,
@@ -135,36 +183,105 @@ __global__ void __launch_bounds__(kSlotAlign) kDensity(const SceneDev* __restric
                                                        const float4* __restrict__ bpos4, float4* __restrict__ vel4,
                                                        float4* __restrict__ aux4) {
     SF_SLOT_PROLOGUE
+    __shared__ float4 tile[kSlotAlign / 32][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (slot == S.slot_off) state[sid].amax_bits = 0u;
     const float4 pi4 = pos4[slot];
-    if (pi4.w == 0.f) return;
+    const bool active = pi4.w != 0.f;
+    const unsigned activeMask = __ballot_sync(0xffffffffu, active);
+    if (activeMask == 0u) return;  // the whole warp is parking slots
     const float3 pi = xyz(pi4);
+    const int3 c = cellOf(S, pi);
     const bool water = pi4.w > 0.f;
-    float d = water ? pi4.w * S.W0 : 0.f;
-    int c = 0, bc = 0;
+    const long long M = L.M;
     unsigned* __restrict__ nb = L.nbr + slot;
     unsigned* __restrict__ bnb = L.bnbr + slot;
-    forEachCell(S, cellOf(S, pi), [&](int cell) {
-        const unsigned j1 = L.cs[cell + 1];
-        for (unsigned j = L.cs[cell]; j < j1; ++j) {
-            const float4 pj = pos4[j];
-            const float3 dij = pi - xyz(pj);
-            if (!inReach(S, dij)) continue;
-            if (c < kMaxNbr) nb[size_t(c) * L.M] = j;
-            ++c;
-            if (water && pj.w > 0.f) d += pj.w * poly6(S, len3(dij));  // label[i] == label[j]
+    int cS = 0, cW = 0, bc = 0;
+    float d = water ? pi4.w * S.W0 : 0.f;
+    auto append = [&](unsigned j, bool sandJ) {
+        if (cS + cW < kMaxNbr) nb[(sandJ ? cS : kMaxNbr - 1 - cW) * M] = j;
+        if (sandJ)
+            ++cS;
+        else
+            ++cW;
+    };
+    auto appendBoundary = [&](unsigned j) {
+        if (bc < kMaxBNbr) bnb[bc * M] = j;
+        ++bc;
+    };
+    const int leader = __ffs(activeMask) - 1;
+    const int cx0 = __shfl_sync(0xffffffffu, c.x, leader), cy0 = __shfl_sync(0xffffffffu, c.y, leader);
+    int zmin = active ? c.z : 0x7fffffff, zmax = active ? c.z : -1;
+    for (int o = 16; o > 0; o >>= 1) {
+        zmin = min(zmin, __shfl_xor_sync(0xffffffffu, zmin, o));
+        zmax = max(zmax, __shfl_xor_sync(0xffffffffu, zmax, o));
+    }
+    const bool column = __all_sync(0xffffffffu, !active || (c.x == cx0 && c.y == cy0)) && zmax - zmin <= 6;
+    if (column) {
+        // warp-cooperative walk: one pass over the union window per (dx, dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+            const int x = cx0 + dx;
+            if (x < 0 || x >= S.gx) continue;
+            for (int dy = -1; dy <= 1; ++dy) {
+                const int y = cy0 + dy;
+                if (y < 0 || y >= S.gy) continue;
+                const int base = S.cell_off + (x * S.gy + y) * S.gz;
+                unsigned lo = 0, hi = 0;
+                if (active) {
+                    lo = L.cs[base + max(c.z - 1, 0)];
+                    hi = L.cs[base + min(c.z + 1, S.gz - 1) + 1];
+                }
+                const unsigned ulo = L.cs[base + max(zmin - 1, 0)];
+                const unsigned uhi = L.cs[base + min(zmax + 1, S.gz - 1) + 1];
+                for (unsigned t0 = ulo; t0 < uhi; t0 += 32) {
+                    const unsigned jl = t0 + lane;
+                    tile[warp][lane] = jl < uhi ? pos4[jl] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    __syncwarp();
+                    const int nt = int(min(32u, uhi - t0));
+                    for (int t = 0; t < nt; ++t) {
+                        const unsigned j = t0 + unsigned(t);
+                        if (j >= lo && j < hi) {
+                            const float4 pj = tile[warp][t];
+                            const float3 dij = pi - xyz(pj);
+                            if (inReach(S, dij)) {
+                                append(j, pj.w < 0.f);
+                                if (water && pj.w > 0.f) d += pj.w * poly6(S, len3(dij));
+                            }
+                        }
+                    }
+                    __syncwarp();
+                }
+                if (active) {
+                    for (int z = max(c.z - 1, 0); z <= min(c.z + 1, S.gz - 1); ++z)
+                        for (unsigned j = L.bcs[base + z]; j < L.bcs[base + z + 1]; ++j)
+                            if (inReach(S, pi - xyz(bpos4[j]))) appendBoundary(j);
+                }
+            }
         }
-        const unsigned b1 = L.bcs[cell + 1];
-        for (unsigned j = L.bcs[cell]; j < b1; ++j) {
-            const float4 bj = bpos4[j];
-            const float3 dij = pi - xyz(bj);
-            if (!inReach(S, dij)) continue;
-            if (bc < kMaxBNbr) bnb[size_t(bc) * L.M] = j;
-            ++bc;
-            if (water) d += S.rho0 * fabsf(bj.w) * poly6(S, len3(dij));
-        }
-    });
-    L.cnt[slot] = c;
+        // near walls the reference interleaves boundary terms cell by cell
+        if (water && bc > 0) d = exactDensity(S, L, pi, pi4.w, pos4, bpos4);
+    } else if (active) {
+        forEachCell(S, c, [&](int cell) {
+            const unsigned j1 = L.cs[cell + 1];
+            for (unsigned j = L.cs[cell]; j < j1; ++j) {
+                const float4 pj = pos4[j];
+                const float3 dij = pi - xyz(pj);
+                if (!inReach(S, dij)) continue;
+                append(j, pj.w < 0.f);
+                if (water && pj.w > 0.f) d += pj.w * poly6(S, len3(dij));  // label[i] == label[j]
+            }
+            const unsigned b1 = L.bcs[cell + 1];
+            for (unsigned j = L.bcs[cell]; j < b1; ++j) {
+                const float4 bj = bpos4[j];
+                const float3 dij = pi - xyz(bj);
+                if (!inReach(S, dij)) continue;
+                appendBoundary(j);
+                if (water) d += S.rho0 * fabsf(bj.w) * poly6(S, len3(dij));
+            }
+        });
+    }
+    if (!active) return;
+    L.cnt[slot] = unsigned(min(cS, 0xFFFF)) | (unsigned(min(cW, 0xFFFF)) << 16);
     L.bcnt[slot] = bc;
     float density, pressure = 0.f;
     if (!water) {
@@ -199,23 +316,30 @@ __global__ void __launch_bounds__(kSlotAlign) kAvgFlow(const SceneDev* __restric
     const bool sandI = pi4.w < 0.f;
     float v_s = 0.f, v_w = 0.f, sand_volume = 0.f;
     float3 avg_s = mk3(0.f, 0.f, 0.f), avg_w = avg_s;
-    forFluidNeighbors(S, L, slot, pi, pos4, [&](int j) {
+    // sand neighbours: sand volume (every i) and, for water i, the sand average flow
+    forSandNeighbors(S, L, slot, pi, pos4, [&](int j) {
         const float4 pj = pos4[j];
-        const float3 dij = pi - xyz(pj);
         const float4 vj4 = vel4[j];
-        const bool sandJ = pj.w < 0.f;
-        const float mj = fabsf(pj.w);
-        const float wij = poly6(S, len3(dij));
-        if (sandJ && vj4.w != 0.f) sand_volume += mj / vj4.w * wij;
-        const float vj = mj / vj4.w;
-        if (sandI && !sandJ) {
-            avg_s += xyz(vj4) * vj * wij;
-            v_s += vj * wij;
-        } else if (!sandI && sandJ) {
+        const float mj = -pj.w;
+        const float wij = poly6(S, len3(pi - xyz(pj)));
+        if (vj4.w != 0.f) sand_volume += mj / vj4.w * wij;
+        if (!sandI) {
+            const float vj = mj / vj4.w;
             avg_w += xyz(vj4) * vj * wij;
             v_w += vj * wij;
         }
     });
+    // water neighbours of sand i: the water average flow and the saturation
+    if (sandI) {
+        forWaterNeighbors(S, L, slot, pi, pos4, [&](int j) {
+            const float4 pj = pos4[j];
+            const float4 vj4 = vel4[j];
+            const float vj = pj.w / vj4.w;
+            const float wij = poly6(S, len3(pi - xyz(pj)));
+            avg_s += xyz(vj4) * vj * wij;
+            v_s += vj * wij;
+        });
+    }
     float3 avg;
     if (!sandI && v_w != 0.f)
         avg = avg_w / v_w;
@@ -247,9 +371,8 @@ __global__ void __launch_bounds__(kSlotAlign) kVoidageAdhesion(
     if (pi4.w < 0.f) {
         const float sat = aux4[slot].z;
         float num = 0.f, den = 0.f;
-        forFluidNeighbors(S, L, slot, pi, pos4, [&](int j) {
+        forWaterNeighbors(S, L, slot, pi, pos4, [&](int j) {
             const float4 pj = pos4[j];
-            if (!(pj.w > 0.f)) return;
             const float3 dij = pi - xyz(pj);
             const float vj = pj.w / vel4[j].w;
             const float wij = poly6(S, len3(dij));
@@ -272,9 +395,8 @@ __global__ void __launch_bounds__(kSlotAlign) kVoidageAdhesion(
         const float mi = pi4.w;
         float v_s = 0.f;
         float3 ad = mk3(0.f, 0.f, 0.f);
-        forFluidNeighbors(S, L, slot, pi, pos4, [&](int j) {
+        forSandNeighbors(S, L, slot, pi, pos4, [&](int j) {
             const float4 pj = pos4[j];
-            if (!(pj.w < 0.f)) return;
             const float3 dpij = pi - xyz(pj);
             const float ldp = len3(dpij);
             const float wij = poly6(S, ldp);
@@ -316,24 +438,24 @@ __global__ void __launch_bounds__(kSlotAlign) kSandMomentum(
     const float vol_i = mi / fmaxf(kEps, di);
     float v_w = 0.f;
     float3 f = mk3(0.f, 0.f, 0.f), df = f;
-    forFluidNeighbors(S, L, slot, pi, pos4, [&](int j) {
+    forSandNeighbors(S, L, slot, pi, pos4, [&](int j) {
+        if (j == slot) return;
+        const float3 dij = xyz(pos4[j]) - pi;
+        if (dot3(dij, dij) >= S.dem_reach2) return;  // both terms are exactly zero beyond contact + bridge
+        f += demForce(dij, xyz(vel4[j]) - vi, S.rij2, S.kn, S.ks, S.tan2);
+        f += capillaryForce(S, dij, (ai.z + aux4[j].z) / 2.f);
+    });
+    forWaterNeighbors(S, L, slot, pi, pos4, [&](int j) {
         const float4 pj = pos4[j];
-        if (pj.w < 0.f) {
-            if (j == slot) return;
-            const float3 dij = xyz(pj) - pi;
-            f += demForce(dij, xyz(vel4[j]) - vi, S.rij2, S.kn, S.ks, S.tan2);
-            f += capillaryForce(S, dij, (ai.z + aux4[j].z) / 2.f);
-        } else {
-            const float3 dij = pi - xyz(pj);
-            const float4 aj = aux4[j];
-            const float wij = poly6(S, len3(dij));
-            if (aj.w > 0.f && aj.w <= 1.f) {
-                const float dj = vel4[j].w / fmaxf(kEps, aj.w);
-                v_w += pj.w / dj * wij;
-                f += -mi * pj.w * aj.x / fmaxf(kEps, di * dj) * spikyGrad(S, dij);
-            }
-            f += wij * vol_i * xyz(avgadh4[j]);
+        const float3 dij = pi - xyz(pj);
+        const float4 aj = aux4[j];
+        const float wij = poly6(S, len3(dij));
+        if (aj.w > 0.f && aj.w <= 1.f) {
+            const float dj = vel4[j].w / fmaxf(kEps, aj.w);
+            v_w += pj.w / dj * wij;
+            f += -mi * pj.w * aj.x / fmaxf(kEps, di * dj) * spikyGrad(S, dij);
         }
+        f += wij * vol_i * xyz(avgadh4[j]);
     });
     if (S.shape_boundary) {
         forBoundaryNeighbors(S, L, slot, pi, bpos4, [&](int b) {
@@ -391,29 +513,30 @@ __global__ void __launch_bounds__(kSlotAlign) kWaterMomentum(
         const float pri = ai4.x;
         const float pterm_i = pri / fmaxf(kEps, di * di);
         float3 a = mk3(0.f, 0.f, 0.f);
-        forFluidNeighbors(S, L, slot, pi, pos4, [&](int j) {
+        forWaterNeighbors(S, L, slot, pi, pos4, [&](int j) {
+            if (j == slot) return;
             const float4 pj = pos4[j];
             const float3 dij = pi - xyz(pj);
-            if (pj.w > 0.f) {
-                if (j == slot) return;
-                const float4 aj = aux4[j];
-                const float4 vj4 = vel4[j];
-                const float dj = vj4.w / fmaxf(kEps, aj.w);
-                const float3 nab = spikyGrad(S, dij);
-                a += -pj.w * (pterm_i + aj.x / fmaxf(kEps, dj * dj)) * nab;
-                const float dd = dot3(vi - xyz(vj4), dij);
-                if (dd < 0.f) {
-                    const float pij = -S.nu / (di + dj) * (dd / (dot3(dij, dij) + kEps));
-                    a += -pj.w * pij * nab;
-                }
-            } else {
-                const float dj = vel4[j].w;
-                const float wij = poly6(S, len3(dij));
-                const float3 nab = spikyGrad(S, dij);
-                const float3 buoy = pj.w * pri / fmaxf(kEps, di * dj) * nab;  // -m_j with m_j = -w
-                const float3 drag = -wij / di * xyz(drag4[j]);
-                a += buoy + drag;
+            const float4 aj = aux4[j];
+            const float4 vj4 = vel4[j];
+            const float dj = vj4.w / fmaxf(kEps, aj.w);
+            const float3 nab = spikyGrad(S, dij);
+            a += -pj.w * (pterm_i + aj.x / fmaxf(kEps, dj * dj)) * nab;
+            const float dd = dot3(vi - xyz(vj4), dij);
+            if (dd < 0.f) {
+                const float pij = -S.nu / (di + dj) * (dd / (dot3(dij, dij) + kEps));
+                a += -pj.w * pij * nab;
             }
+        });
+        forSandNeighbors(S, L, slot, pi, pos4, [&](int j) {
+            const float4 pj = pos4[j];
+            const float3 dij = pi - xyz(pj);
+            const float dj = vel4[j].w;
+            const float wij = poly6(S, len3(dij));
+            const float3 nab = spikyGrad(S, dij);
+            const float3 buoy = pj.w * pri / fmaxf(kEps, di * dj) * nab;  // -m_j with m_j = -w
+            const float3 drag = -wij / di * xyz(drag4[j]);
+            a += buoy + drag;
         });
         const float bp = pri / fmaxf(kEps, S.rho0 * S.rho0);
         const float bvis = -S.bnu / (2.f * S.rho0);

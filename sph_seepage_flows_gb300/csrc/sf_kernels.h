@@ -20,11 +20,15 @@ struct LaunchCtx {
 };
 
 // Neighbour lists of the current substep (column-major: entry k of slot i at
-// k * M + i). A count above the capacity means "walk the stencil instead".
+// k * M + i). Particle lists hold sand neighbours from entry 0 upwards and
+// water neighbours from entry kMaxNbr - 1 downwards; cnt packs the two counts
+// (sand in the low 16 bits, each saturating at 0xFFFF). Counts summing above
+// kMaxNbr mean the list overflowed: walk the stencil instead. A boundary count
+// above kMaxBNbr means the same for the boundary list.
 constexpr int kMaxNbr = 64;
 constexpr int kMaxBNbr = 48;
 struct NbrLists {
-    const int* cnt;
+    const unsigned int* cnt;
     const unsigned int* nbr;
     const int* bcnt;
     const unsigned int* bnbr;
@@ -33,7 +37,7 @@ struct NbrLists {
     long long M;              // total slots
 };
 struct NbrListsW {
-    int* cnt;
+    unsigned int* cnt;
     unsigned int* nbr;
     int* bcnt;
     unsigned int* bnbr;

@@ -32,6 +32,7 @@ FIELDS = {
     "avg_drag": (13, 3, np.float32), "adhesion": (14, 3, np.float32),
     "avg_adhesion": (15, 3, np.float32), "cda0asat": (16, 3, np.float32),
     "amcamcp": (17, 2, np.float32), "id": (18, 1, np.int32), "key": (19, 1, np.int32),
+    "neighbors": (20, 1, np.int32),
 }
 BFIELDS = {"bpos": (32, 3, np.float32), "blabel": (33, 1, np.int32), "bvolume": (34, 1, np.float32)}
 

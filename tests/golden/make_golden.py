@@ -25,7 +25,7 @@ from sph_seepage_flows_gb300 import scenes  # noqa: E402
 from sph_seepage_flows_gb300.params import FIELDS, SF_SOLVER_SPH, SF_TYPE_SF  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
-FIELD_NAMES = [k for k in FIELDS if k != "key"]
+FIELD_NAMES = [k for k in FIELDS if k not in ("key", "neighbors")]
 
 
 def cast(name, a):

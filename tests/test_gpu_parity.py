@@ -132,8 +132,14 @@ def test_stages_bit_exact_against_fp32_oracle(cuda_lib, oracle_mod, which):
                     water = sim.field("label") == 0
                     got, ref = got[water], ref[water]
                 frac = exact_fraction(got, ref)
+                scale = None
+                if name == "acc" and st in ("sand_momentum", "water_momentum"):
+                    # cancelling sums: measure against the sum of term magnitudes
+                    keep = (sim.field("label") == (1 if st == "sand_momentum" else 0))
+                    scale = o32.field("acc_scale")[keep]
                 if name in transcendental:
-                    assert rel_err(got, ref) <= TOL, (rep, st, name, rel_err(got, ref))
+                    err = rel_err(got, ref, scale)
+                    assert err <= TOL, (rep, st, name, err)
                 else:
                     assert frac == 1.0, (rep, st, name, frac, rel_err(got, ref))
             # continue both from the GPU state so every stage sees identical inputs

@@ -9,7 +9,7 @@ from sph_seepage_flows_gb300 import scenes
 from sph_seepage_flows_gb300.params import FIELDS
 
 T = 1.0 / 30.0
-NAMES = [k for k in FIELDS if k != "key"]
+NAMES = [k for k in FIELDS if k not in ("key", "neighbors")]
 
 
 @pytest.mark.parametrize("fixture", ["tiny_multi_wcsph.npz", "tiny_sf_sph.npz"])

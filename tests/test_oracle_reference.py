@@ -41,7 +41,7 @@ def test_oracle_bit_exact_with_reference_kernels(harness, name, kw, override):
         assert o.num_substeps == ref.num_substeps
         assert np.array_equal(o.cell_table(0), ref.cell_table(0))
         for f in FIELDS:
-            if f == "key":
+            if f in ("key", "neighbors"):
                 continue
             assert np.array_equal(o.field(f), ref.field(f)), (step, f)
 
