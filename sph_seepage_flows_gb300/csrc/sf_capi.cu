@@ -188,6 +188,8 @@ struct sf_handle {
     unsigned int *keys = nullptr, *cs = nullptr, *bcs = nullptr;
     unsigned int* nbrCnt = nullptr;
     int* bnbrCnt = nullptr;
+    int* cnbrCnt = nullptr;
+    unsigned int* cnbr = nullptr;
     unsigned int *nbr = nullptr, *bnbr = nullptr;
     unsigned int* sortedKeys = nullptr;  // points into keys/scratch after a sort
     SortScratch sc{};
@@ -226,6 +228,8 @@ struct sf_handle {
         b.listsW.nbr = nbr;
         b.listsW.bcnt = bnbrCnt;
         b.listsW.bnbr = bnbr;
+        b.listsW.ccnt = cnbrCnt;
+        b.listsW.cnbr = cnbr;
         b.listsW.cs = cs;
         b.listsW.bcs = bcs;
         b.listsW.M = totalSlots;
@@ -233,6 +237,8 @@ struct sf_handle {
         b.lists.nbr = nbr;
         b.lists.bcnt = bnbrCnt;
         b.lists.bnbr = bnbr;
+        b.lists.ccnt = cnbrCnt;
+        b.lists.cnbr = cnbr;
         b.lists.cs = cs;
         b.lists.bcs = bcs;
         b.lists.M = totalSlots;
@@ -271,6 +277,8 @@ struct sf_handle {
         devFree(bnbrCnt);
         devFree(nbr);
         devFree(bnbr);
+        devFree(cnbrCnt);
+        devFree(cnbr);
         devFree(cs);
         devFree(bcs);
         devFree(sc.keysAlt);
@@ -470,6 +478,8 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
     SF_ALLOC(h->bnbrCnt, sizeof(int) * M);
     SF_ALLOC(h->nbr, sizeof(unsigned) * M * kMaxNbr);
     SF_ALLOC(h->bnbr, sizeof(unsigned) * M * kMaxBNbr);
+    SF_ALLOC(h->cnbrCnt, sizeof(int) * M);
+    SF_ALLOC(h->cnbr, sizeof(unsigned) * M * kMaxContact);
     SF_ALLOC(h->sc.keysAlt, sizeof(unsigned) * M);
     SF_ALLOC(h->sc.vals, sizeof(unsigned) * M);
     SF_ALLOC(h->sc.valsAlt, sizeof(unsigned) * M);

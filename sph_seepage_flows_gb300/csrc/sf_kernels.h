@@ -27,11 +27,16 @@ struct LaunchCtx {
 // above kMaxBNbr means the same for the boundary list.
 constexpr int kMaxNbr = 64;
 constexpr int kMaxBNbr = 48;
+// Sand-sand pairs within DEM contact + liquid-bridge reach of a sand particle
+// (the only pairs with DEM or capillary forces); more means "filter the sand list".
+constexpr int kMaxContact = 16;
 struct NbrLists {
     const unsigned int* cnt;
     const unsigned int* nbr;
     const int* bcnt;
     const unsigned int* bnbr;
+    const int* ccnt;
+    const unsigned int* cnbr;
     const unsigned int* cs;   // particle cell table (total_cells + 1)
     const unsigned int* bcs;  // boundary cell table (total_cells + 1)
     long long M;              // total slots
@@ -41,6 +46,8 @@ struct NbrListsW {
     unsigned int* nbr;
     int* bcnt;
     unsigned int* bnbr;
+    int* ccnt;
+    unsigned int* cnbr;
     const unsigned int* cs;
     const unsigned int* bcs;
     long long M;

@@ -4,8 +4,8 @@ Individual trajectories of a collapsing granular/fluid system diverge from
 FP32 rounding differences, so single-particle extremes (the maximum
 saturation) drift by a few percent; the bar is on aggregates: total mass
 exact, kinetic energy within 1% (floor: 1% of the run's peak KE), and the
-saturation field's mean, 90th percentile and wet fraction (saturation > 0.01)
-within 1% (floor 1e-3)."""
+saturation field's mean and 90th percentile within 1% (floor 1e-3) and its
+wet fraction (saturation > 0.01) within 1% or 5 particles."""
 
 import numpy as np
 import pytest
@@ -45,5 +45,8 @@ def test_thousand_substeps_statistics(cuda_lib, oracle_mod):
     for a, b in zip(g_series, o_series):
         assert a["mass"] == pytest.approx(b["mass"], rel=1e-6)
         assert abs(a["ke"] - b["ke"]) <= 0.01 * max(abs(b["ke"]), 0.01 * peak_ke)
-        for k in ("sat_mean", "sat_p90", "wet_frac"):
+        for k in ("sat_mean", "sat_p90"):
             assert abs(a[k] - b[k]) <= 0.01 * max(b[k], 1e-3), (k, a[k], b[k])
+        # a count: 1% of the wet fraction, but never less than 5 particles
+        assert abs(a["wet_frac"] - b["wet_frac"]) <= max(0.01 * b["wet_frac"], 5.0 / sc.n_sand), \
+            ("wet_frac", a["wet_frac"], b["wet_frac"])
