@@ -73,8 +73,18 @@ __device__ __forceinline__ void forLabelNeighbors(const SceneDev& S, const NbrLi
         const int n = kSand ? int(c & 0xFFFFu) : int(c >> 16);
         const unsigned* __restrict__ p = L.nbr + slot + (kSand ? 0 : size_t(kMaxNbr - 1) * L.M);
         const long long step = kSand ? L.M : -L.M;
-#pragma unroll 2
-        for (int k = 0; k < n; ++k) f(int(p[k * step]));
+        // indices are loaded a group ahead so the neighbour gathers of
+        // consecutive entries overlap
+        int k = 0;
+        for (; k + 4 <= n; k += 4) {
+            const int j0 = int(p[k * step]), j1 = int(p[(k + 1) * step]);
+            const int j2 = int(p[(k + 2) * step]), j3 = int(p[(k + 3) * step]);
+            f(j0);
+            f(j1);
+            f(j2);
+            f(j3);
+        }
+        for (; k < n; ++k) f(int(p[k * step]));
     } else {
         // stencil walk in the same order: 9 (dx, dy) columns, 3 contiguous z-cells each
         const int3 c = cellOf(S, pi);
@@ -230,22 +240,35 @@ __global__ void __launch_bounds__(kSlotAlign) kDensity(const SceneDev* __restric
             if (y < 0 || y >= S.gy) continue;
             const int base = S.cell_off + (x * S.gy + y) * S.gz;
             const unsigned jEnd = L.cs[base + z1];
-#pragma unroll 2
-            for (unsigned j = L.cs[base + z0]; j < jEnd; ++j) {
-                const float4 pj = pos4[j];
-                const float3 dij = pi - xyz(pj);
-                if (!inReachFast(S, dij)) continue;
-                const bool sandJ = pj.w < 0.f;
-                if (cS + cW < kMaxNbr) nb[(sandJ ? cS : kMaxNbr - 1 - cW) * M] = j;
-                if (sandJ) {
-                    ++cS;
-                    if (!water && j != unsigned(slot) && dot3(dij, dij) < S.dem_reach2) {
-                        if (cc < kMaxContact) cnb[cc * M] = j;
-                        ++cc;
+            // chunks of up to 32 candidates: a branch-free pass marks the
+            // candidates in reach, then the marked ones are appended in order
+#pragma unroll 1
+            for (unsigned j0 = L.cs[base + z0]; j0 < jEnd; j0 += 32u) {
+                const int n = int(min(32u, jEnd - j0));
+                unsigned hit = 0u;
+#pragma unroll 4
+                for (int t = 0; t < n; ++t)
+                    hit |= unsigned(inReachFast(S, pi - xyz(pos4[j0 + unsigned(t)]))) << t;
+                while (hit) {
+                    const int t = __ffs(hit) - 1;
+                    hit &= hit - 1u;
+                    const unsigned j = j0 + unsigned(t);
+                    const float4 pj = pos4[j];
+                    const bool sandJ = pj.w < 0.f;
+                    if (cS + cW < kMaxNbr) nb[(sandJ ? cS : kMaxNbr - 1 - cW) * M] = j;
+                    if (sandJ) {
+                        ++cS;
+                        if (!water && j != unsigned(slot)) {
+                            const float3 dij = pi - xyz(pj);
+                            if (dot3(dij, dij) < S.dem_reach2) {
+                                if (cc < kMaxContact) cnb[cc * M] = j;
+                                ++cc;
+                            }
+                        }
+                    } else {
+                        ++cW;
+                        if (water) d += pj.w * poly6(S, len3(pi - xyz(pj)));  // label[i] == label[j]
                     }
-                } else {
-                    ++cW;
-                    if (water) d += pj.w * poly6(S, len3(dij));  // label[i] == label[j]
                 }
             }
             const unsigned bEnd = L.bcs[base + z1];
