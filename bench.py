@@ -53,6 +53,11 @@ STAGE_BYTES = {
 }
 BYTES_PER_SUBSTEP = sum(STAGE_BYTES.values())  # 753
 
+# DRAM bytes (read + write) per launch of each stage's main kernel on the 1M
+# workload, from the committed ncu capture (profiles/neighbor_passes_1M_ncu.md).
+NCU_TRAFFIC = {"density": 309.2e6, "avgflow": 116.8e6, "water_momentum": 128.8e6,
+               "sand_momentum": 54.6e6, "voidage_adhesion": 41.8e6}
+
 
 def peaks():
     try:
@@ -329,7 +334,9 @@ def run_ours(args, rank, world):
                    "l2": "working set ~250 B/particle > L2 (no flush needed)" if n >= 600_000 else "flushed",
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": NCU_TRAFFIC.get(top) if args.workload == "plain_large" else None,
+                     "traffic_source": "profiles/neighbor_passes_1M_ncu.md (dram read + write per launch)",
                      "algorithmic_bytes_per_particle": STAGE_BYTES[top]},
         "substep_roofline_frac": BYTES_PER_SUBSTEP * n / (ms / steps * 1e-3) / 1e9 / peak,
         "stage_ms": stage_ms,
