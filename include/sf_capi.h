@@ -24,6 +24,7 @@
  *   sf_run_stage         the protected per-pass methods of CudaSphSFSolver (src/kiri_pbs_cuda/solver/seepage_flow/cuda_sph_sf_solver.cu:20-402)
  *   sf_substeps_fixed    fixed-substep mode of main.cpp:250-258 (no reference counterpart for the graph capture)
  *   sf_create_batched    no reference counterpart (independent scenes in one launch)
+ *   sf_adjoint_run       no reference counterpart (reverse-mode gradient of a trajectory loss)
  *
  * Threading: handles are independent; one handle must not be used from two
  * host threads at once. All work is issued on the stream given at creation.
@@ -253,6 +254,35 @@ sf_status sf_set_tuning(sf_handle* h, int32_t block_size, int32_t items_per_thre
 
 /* Text of the last error on this handle (or of the last failed create when h is NULL). */
 const char* sf_last_error_string(const sf_handle* h);
+
+/* Gradient of a trajectory loss by reverse-mode differentiation (no reference
+ * counterpart: the reference has no adjoint).
+ *
+ * Runs n_substeps substeps of every scene at the fixed dt from the current
+ * state (the same trajectory sf_substeps_fixed computes), evaluates per scene
+ *     L = (1 / N_sand) * sum over sand particles of |x_T - target|^2
+ * and back-propagates it through every substep. State is checkpointed every
+ * checkpoint_every substeps and recomputed segment by segment, so device
+ * memory grows with n_substeps / checkpoint_every + checkpoint_every states
+ * (76 bytes per slot each).
+ *
+ * Arrays are scene-major over the handle's scenes and ordered by particle id
+ * within a scene (the creation order), 3 floats per particle:
+ *   target_pos       in:  sum(n) * 3 target positions (water entries unused)
+ *   loss_out         out: n_scenes losses
+ *   grad_params_out  out: n_scenes * 3: dL/d tan(friction angle), dL/d capillary
+ *                         scale (a factor on c0, cmc, csat), dL/d permeability
+ *                         scale (a factor on cd), each at its current value   (may be NULL)
+ *   grad_pos0_out    out: sum(n) * 3: dL/d initial positions                    (may be NULL)
+ *   grad_vel0_out    out: sum(n) * 3: dL/d initial velocities                   (may be NULL)
+ *   ms_out           out: [forward ms, reverse ms] of device time               (may be NULL)
+ * All pointers are host memory. On return the handle holds the final state
+ * x_T, v_T; the per-substep fields (density, pressure, ...) hold the values of
+ * the first substep until the next substep runs. The push-out of water from
+ * shape-boundary particles (label 1) is held constant in the gradient. */
+sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t checkpoint_every,
+                         const float* target_pos, float* loss_out, float* grad_params_out,
+                         float* grad_pos0_out, float* grad_vel0_out, float* ms_out);
 
 #ifdef __cplusplus
 }

@@ -81,6 +81,7 @@ def load(path: str = LIB_PATH):
         "sf_launch_count": (i32, [H, P(i64)]),
         "sf_set_tuning": (i32, [H, i32, i32]),
         "sf_last_error_string": (ctypes.c_char_p, [H]),
+        "sf_adjoint_run": (i32, [H, f32, i64, i64, P(f32), P(f32), P(f32), P(f32), P(f32), P(f32)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -243,6 +244,29 @@ class Simulation:
         self._check(self.lib.sf_get_cell_table(self.h, scene, which,
                                                out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), out.size))
         return out
+
+    # -------------------------------------------------------------- adjoint
+    def adjoint(self, dt: float, n_substeps: int, target, checkpoint_every: int = 1,
+                want_state_grads: bool = True) -> dict:
+        """Runs n_substeps at the fixed dt and back-propagates the per-scene loss
+        mean_sand |x_T - target|^2 (sf_adjoint_run). target: (sum n, 3), scene-major,
+        id order. Returns loss (n_scenes,), grad_params (n_scenes, 3: tan friction
+        angle, capillary scale, permeability scale), grad_pos0 / grad_vel0
+        (sum n, 3, id order) and the forward / reverse device milliseconds."""
+        ns = len(self.scenes)
+        total = sum(self.size(s) for s in range(ns))
+        tgt = np.ascontiguousarray(target, dtype=np.float32).reshape(-1)
+        if tgt.size != 3 * total:
+            raise ValueError(f"target must hold {total} x 3 floats")
+        loss = np.zeros(ns, np.float32)
+        gp = np.zeros((ns, 3), np.float32)
+        gx = np.zeros((total, 3), np.float32) if want_state_grads else None
+        gv = np.zeros((total, 3), np.float32) if want_state_grads else None
+        ms = np.zeros(2, np.float32)
+        self._check(self.lib.sf_adjoint_run(self.h, float(dt), int(n_substeps), int(checkpoint_every), _fptr(tgt),
+                                            _fptr(loss), _fptr(gp), _fptr(gx), _fptr(gv), _fptr(ms)))
+        return {"loss": loss, "grad_params": gp, "grad_pos0": gx, "grad_vel0": gv,
+                "ms_forward": float(ms[0]), "ms_reverse": float(ms[1])}
 
     def add_sph_particles(self, pos, col, vel, mass: float, radius: float, scene: int = 0):
         p = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)

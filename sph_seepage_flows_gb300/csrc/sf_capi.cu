@@ -5,6 +5,7 @@
 // CUDA graphs of two substeps (the persistent arrays ping-pong between two
 // buffer sets at every sort, so two substeps return to the same buffers).
 #include "../../include/sf_capi.h"
+#include "sf_adjoint.h"
 #include "sf_device.cuh"
 #include "sf_kernels.h"
 
@@ -201,6 +202,13 @@ struct sf_handle {
     bool sorted = false;
     int64_t launches = 0;
     GraphCache graph[2];
+    // reverse-mode buffers, allocated by the first sf_adjoint_run
+    AdjBuffers adj{};
+    float* adjTarget = nullptr;   // 3 floats per slot, indexed by slot_off + id
+    float* adjParam = nullptr;    // 3 per slot block
+    float2* adjLoss = nullptr;    // 1 per slot block
+    char* snap = nullptr;         // state snapshots for checkpointing
+    size_t snapBytes = 0;
     std::string err;
 
     sf_status fail(sf_status st, const std::string& msg) {
@@ -292,6 +300,13 @@ struct sf_handle {
         devFree(dBlockScene);
         devFree(dState);
         devFree(dErr);
+        for (float4** p : {&adj.adjX, &adj.adjV, &adj.x, &adj.v, &adj.acc, &adj.flow, &adj.adh, &adj.avgadh,
+                           &adj.drag, &adj.f, &adj.r, &adj.s})
+            devFree(*p);
+        devFree(adjTarget);
+        devFree(adjParam);
+        devFree(adjLoss);
+        devFree(snap);
         if (stage) cudaFree(stage);
         if (ownStream && stream) cudaStreamDestroy(stream);
     }
@@ -1024,5 +1039,188 @@ sf_status sf_set_tuning(sf_handle* h, int32_t block_size, int32_t items_per_thre
 }
 
 const char* sf_last_error_string(const sf_handle* h) { return h ? h->err.c_str() : g_createError.c_str(); }
+
+// ---------------------------------------------------------------- adjoint
+namespace {
+
+// One snapshot = the persistent per-slot arrays of the current buffer set
+// (pos, vel, col, mat, amc, pid), which fully determine the next substeps
+// including the summation order of the stable sort.
+size_t snapStride(const sf_handle* h) {
+    return size_t(h->totalSlots) * (4 * sizeof(float4) + sizeof(float2) + sizeof(int));
+}
+
+sf_status snapCopy(sf_handle* h, char* snap, bool save) {
+    const size_t M = size_t(h->totalSlots);
+    const int c = h->cur;
+    void* arrays[6] = {h->pos[c], h->vel[c], h->col[c], h->mat[c], h->amc[c], h->pid[c]};
+    const size_t bytes[6] = {sizeof(float4) * M, sizeof(float4) * M, sizeof(float4) * M,
+                             sizeof(float4) * M, sizeof(float2) * M, sizeof(int) * M};
+    size_t off = 0;
+    for (int k = 0; k < 6; ++k) {
+        void* dst = save ? static_cast<void*>(snap + off) : arrays[k];
+        const void* src = save ? arrays[k] : static_cast<const void*>(snap + off);
+        if (h->cuda(cudaMemcpyAsync(dst, src, bytes[k], cudaMemcpyDeviceToDevice, h->stream), "snapshot copy"))
+            return SF_ERR_CUDA;
+        off += bytes[k];
+    }
+    return SF_OK;
+}
+
+sf_status ensureAdjoint(sf_handle* h, size_t snapshots) {
+    const size_t M = size_t(h->totalSlots);
+    if (!h->adj.adjX) {
+        for (float4** p : {&h->adj.adjX, &h->adj.adjV, &h->adj.x, &h->adj.v, &h->adj.acc, &h->adj.flow, &h->adj.adh,
+                           &h->adj.avgadh, &h->adj.drag, &h->adj.f, &h->adj.r, &h->adj.s}) {
+            if (h->cuda(cudaMalloc(reinterpret_cast<void**>(p), sizeof(float4) * M), "cudaMalloc adjoint") ||
+                h->cuda(cudaMemsetAsync(*p, 0, sizeof(float4) * M, h->stream), "cudaMemset adjoint"))
+                return SF_ERR_CUDA;
+        }
+        if (h->cuda(cudaMalloc(reinterpret_cast<void**>(&h->adjTarget), sizeof(float) * 3 * M), "cudaMalloc target") ||
+            h->cuda(cudaMalloc(reinterpret_cast<void**>(&h->adjParam), sizeof(float) * 3 * size_t(h->slotBlocks)),
+                    "cudaMalloc param partials") ||
+            h->cuda(cudaMalloc(reinterpret_cast<void**>(&h->adjLoss), sizeof(float2) * size_t(h->slotBlocks)),
+                    "cudaMalloc loss partials") ||
+            h->cuda(cudaMemsetAsync(h->adjTarget, 0, sizeof(float) * 3 * M, h->stream), "cudaMemset target"))
+            return SF_ERR_CUDA;
+    }
+    const size_t need = snapshots * snapStride(h);
+    if (h->snapBytes < need) {
+        if (h->snap && h->cuda(cudaStreamSynchronize(h->stream), "sync before snapshot realloc")) return SF_ERR_CUDA;
+        devFree(h->snap);
+        h->snapBytes = 0;
+        if (h->cuda(cudaMalloc(reinterpret_cast<void**>(&h->snap), need), "cudaMalloc snapshots")) return SF_ERR_CUDA;
+        h->snapBytes = need;
+    }
+    return SF_OK;
+}
+
+}  // namespace
+
+sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t checkpoint_every,
+                         const float* target_pos, float* loss_out, float* grad_params_out, float* grad_pos0_out,
+                         float* grad_vel0_out, float* ms_out) {
+    if (!h) return SF_ERR_INVALID;
+    if (!target_pos || !loss_out) return h->fail(SF_ERR_INVALID, "target_pos and loss_out are required");
+    if (!(dt > 0.f) || !std::isfinite(dt)) return h->fail(SF_ERR_INVALID, "dt must be finite and > 0");
+    if (n_substeps < 1) return h->fail(SF_ERR_INVALID, "n_substeps must be >= 1");
+    if (checkpoint_every < 1) return h->fail(SF_ERR_INVALID, "checkpoint_every must be >= 1");
+    const int64_t T = n_substeps, K = std::min(checkpoint_every, n_substeps);
+    const int64_t nSeg = (T + K - 1) / K;
+    // snapshot slots: [0, nSeg) checkpoints, then states 1 .. K-1 of a segment, then the final state
+    const int64_t nSnap = nSeg + (K - 1) + 1;
+    if (ensureAdjoint(h, size_t(nSnap))) return SF_ERR_CUDA;
+    const size_t stride = snapStride(h);
+    auto snapAt = [&](int64_t k) { return h->snap + size_t(k) * stride; };
+    char* finalSnap = snapAt(nSnap - 1);
+
+    // targets into the slot_off + id layout
+    int64_t off = 0;
+    for (int s = 0; s < h->nScenes; ++s) {
+        const int64_t n = h->n[s];
+        if (n > 0 && h->cuda(cudaMemcpyAsync(h->adjTarget + 3 * size_t(h->hScenes[s].slot_off), target_pos + 3 * off,
+                                             sizeof(float) * 3 * size_t(n), cudaMemcpyHostToDevice, h->stream),
+                             "target H2D"))
+            return SF_ERR_CUDA;
+        off += n;
+    }
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    for (auto& e : ev)
+        if (h->cuda(cudaEventCreate(&e), "event create")) return SF_ERR_CUDA;
+    struct EventGuard {
+        cudaEvent_t* e;
+        ~EventGuard() {
+            for (int k = 0; k < 3; ++k)
+                if (e[k]) cudaEventDestroy(e[k]);
+        }
+    } guard{ev};
+    cudaEventRecord(ev[0], h->stream);
+
+    // forward pass with a checkpoint at the start of every segment
+    sf_status st = SF_OK;
+    for (int64_t seg = 0; seg < nSeg; ++seg) {
+        if ((st = snapCopy(h, snapAt(seg), true))) return st;
+        if ((st = sf_substeps_fixed(h, dt, std::min(K, T - seg * K)))) return st;
+    }
+    LaunchCtx c = h->ctx();
+    launchAdjSeed(c, h->pos[h->cur], h->pid[h->cur], h->adjTarget, h->adj.adjX, h->adj.adjV, h->adjLoss);
+    h->launches += 1;
+    if ((st = snapCopy(h, finalSnap, true))) return st;
+    if (h->cuda(cudaMemsetAsync(h->adjParam, 0, sizeof(float) * 3 * size_t(h->slotBlocks), h->stream),
+                "clear parameter partials"))
+        return SF_ERR_CUDA;
+    cudaEventRecord(ev[1], h->stream);
+
+    // reverse pass, segment by segment
+    for (int64_t seg = nSeg - 1; seg >= 0; --seg) {
+        const int64_t len = std::min(K, T - seg * K);
+        if (len > 1) {  // states of the segment's substeps 1 .. len-1
+            if ((st = snapCopy(h, snapAt(seg), false))) return st;
+            for (int64_t t = 1; t < len; ++t) {
+                if ((st = runSubstep(h, dt, 0))) return st;
+                if ((st = snapCopy(h, snapAt(nSeg + t - 1), true))) return st;
+            }
+        }
+        for (int64_t t = len - 1; t >= 0; --t) {
+            if ((st = snapCopy(h, t == 0 ? snapAt(seg) : snapAt(nSeg + t - 1), false))) return st;
+            for (int s = SF_STAGE_SORT; s <= SF_STAGE_WATER_MOMENTUM; ++s)
+                if ((st = runStage(h, s, dt, 0))) return st;
+            h->launches += launchAdjSubstep(h->ctx(), h->adj, h->buffers(), h->pid[h->cur], dt, h->adjParam);
+            if (h->cuda(cudaGetLastError(), "adjoint launch")) return SF_ERR_CUDA;
+        }
+    }
+    cudaEventRecord(ev[2], h->stream);
+    if ((st = snapCopy(h, finalSnap, false))) return st;
+
+    // per-scene reductions in block order, and the id-ordered gradients
+    std::vector<float2> lossPart(size_t(h->slotBlocks));
+    std::vector<float> paramPart(3 * size_t(h->slotBlocks));
+    std::vector<float4> gx, gv;
+    if (h->cuda(cudaMemcpyAsync(lossPart.data(), h->adjLoss, sizeof(float2) * lossPart.size(), cudaMemcpyDeviceToHost,
+                                h->stream),
+                "loss D2H") ||
+        h->cuda(cudaMemcpyAsync(paramPart.data(), h->adjParam, sizeof(float) * paramPart.size(),
+                                cudaMemcpyDeviceToHost, h->stream),
+                "parameter gradient D2H") ||
+        h->cuda(cudaStreamSynchronize(h->stream), "adjoint sync"))
+        return SF_ERR_CUDA;
+    off = 0;
+    for (int s = 0; s < h->nScenes; ++s) {
+        const SceneDev& S = h->hScenes[s];
+        double l = 0.0, ns = 0.0, g[3] = {0.0, 0.0, 0.0};
+        for (int b = S.slot_off / kSlotAlign; b < (S.slot_off + S.slot_cap) / kSlotAlign; ++b) {
+            l += lossPart[size_t(b)].x;
+            ns += lossPart[size_t(b)].y;
+            for (int k = 0; k < 3; ++k) g[k] += paramPart[3 * size_t(b) + size_t(k)];
+        }
+        const double inv = ns > 0.0 ? 1.0 / ns : 0.0;
+        loss_out[s] = float(l * inv);
+        if (grad_params_out)
+            for (int k = 0; k < 3; ++k) grad_params_out[3 * s + k] = float(g[k] * inv);
+        const int64_t n = h->n[s];
+        for (int which = 0; which < 2; ++which) {
+            float* out = which ? grad_vel0_out : grad_pos0_out;
+            if (!out || n == 0) continue;
+            std::vector<float4>& buf = which ? gv : gx;
+            buf.resize(size_t(n));
+            if (h->cuda(cudaMemcpyAsync(buf.data(), (which ? h->adj.adjV : h->adj.adjX) + S.slot_off,
+                                        sizeof(float4) * size_t(n), cudaMemcpyDeviceToHost, h->stream),
+                        "gradient D2H") ||
+                h->cuda(cudaStreamSynchronize(h->stream), "gradient sync"))
+                return SF_ERR_CUDA;
+            for (int64_t i = 0; i < n; ++i) {
+                out[3 * (off + i)] = float(double(buf[size_t(i)].x) * inv);
+                out[3 * (off + i) + 1] = float(double(buf[size_t(i)].y) * inv);
+                out[3 * (off + i) + 2] = float(double(buf[size_t(i)].z) * inv);
+            }
+        }
+        off += n;
+    }
+    if (ms_out) {
+        cudaEventElapsedTime(&ms_out[0], ev[0], ev[1]);
+        cudaEventElapsedTime(&ms_out[1], ev[1], ev[2]);
+    }
+    return h->cuda(cudaGetLastError(), "sf_adjoint_run");
+}
 
 }  // extern "C"

@@ -14,10 +14,10 @@
 // stencil candidates), one label class at a time (no label divergence). A
 // particle whose list overflows falls back to the stencil walk.
 //
-// The walk itself is warp-cooperative when the warp's particles share one
-// cell column: the warp streams the union of its members' z-windows through
-// shared memory once per column, each lane keeping the candidates of its own
-// window, so every lane sees its candidates in stencil order.
+// Each thread walks its own stencil as 9 contiguous ranges (the 3 z-cells
+// of one (dx, dy) column are adjacent in the sorted order); a branch-free
+// pass over each chunk of 32 candidates marks those in reach, and only the
+// marked ones are processed, in stencil order.
 //
 // Summation order. Every accumulator of the density, average-flow, voidage,
 // saturation and adhesion passes receives one label class of neighbours, in
@@ -30,6 +30,7 @@
 // magnitudes).
 #include "sf_device.cuh"
 #include "sf_kernels.h"
+#include "sf_neighbors.cuh"
 
 namespace sfg {
 
@@ -37,99 +38,6 @@ namespace sfg {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;                \
     const int sid = blockScene[(blockIdx.x * blockDim.x) / kSlotAlign];    \
     const SceneDev& S = scenes[sid];
-
-// 27-cell stencil of the reference, with the global cell index of cell m.
-template <typename F>
-__device__ __forceinline__ void forEachCell(const SceneDev& S, int3 c, F&& f) {
-#pragma unroll 1
-    for (int dx = -1; dx <= 1; ++dx) {
-        const int x = c.x + dx;
-        if (x < 0 || x >= S.gx) continue;
-#pragma unroll 1
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int y = c.y + dy;
-            if (y < 0 || y >= S.gy) continue;
-            const int base = S.cell_off + (x * S.gy + y) * S.gz;
-#pragma unroll 1
-            for (int dz = -1; dz <= 1; ++dz) {
-                const int z = c.z + dz;
-                if (z < 0 || z >= S.gz) continue;
-                f(base + z);
-            }
-        }
-    }
-}
-
-__device__ __forceinline__ bool inReach(const SceneDev& S, float3 d) { return dot3(d, d) < S.reach2; }
-
-// Neighbours of one label within reach of slot, in stencil order: the sand
-// part (kSand) or the water part of the list, or the stencil when the list
-// overflowed.
-template <bool kSand, typename F>
-__device__ __forceinline__ void forLabelNeighbors(const SceneDev& S, const NbrLists& L, int slot, float3 pi,
-                                                  const float4* __restrict__ pos4, F&& f) {
-    const unsigned c = L.cnt[slot];
-    if (int(c & 0xFFFFu) + int(c >> 16) <= kMaxNbr) {
-        const int n = kSand ? int(c & 0xFFFFu) : int(c >> 16);
-        const unsigned* __restrict__ p = L.nbr + slot + (kSand ? 0 : size_t(kMaxNbr - 1) * L.M);
-        const long long step = kSand ? L.M : -L.M;
-        // indices are loaded a group ahead so the neighbour gathers of
-        // consecutive entries overlap
-        int k = 0;
-        for (; k + 4 <= n; k += 4) {
-            const int j0 = int(p[k * step]), j1 = int(p[(k + 1) * step]);
-            const int j2 = int(p[(k + 2) * step]), j3 = int(p[(k + 3) * step]);
-            f(j0);
-            f(j1);
-            f(j2);
-            f(j3);
-        }
-        for (; k < n; ++k) f(int(p[k * step]));
-    } else {
-        // stencil walk in the same order: 9 (dx, dy) columns, 3 contiguous z-cells each
-        const int3 c = cellOf(S, pi);
-        const int z0 = max(c.z - 1, 0), z1 = min(c.z + 1, S.gz - 1) + 1;
-        for (int x = max(c.x - 1, 0); x <= min(c.x + 1, S.gx - 1); ++x)
-            for (int y = max(c.y - 1, 0); y <= min(c.y + 1, S.gy - 1); ++y) {
-                const int base = S.cell_off + (x * S.gy + y) * S.gz;
-                for (unsigned j = L.cs[base + z0]; j < L.cs[base + z1]; ++j) {
-                    const float4 pj = pos4[j];
-                    if ((kSand ? pj.w < 0.f : pj.w > 0.f) && inReach(S, pi - xyz(pj))) f(int(j));
-                }
-            }
-    }
-}
-template <typename F>
-__device__ __forceinline__ void forSandNeighbors(const SceneDev& S, const NbrLists& L, int slot, float3 pi,
-                                                 const float4* __restrict__ pos4, F&& f) {
-    forLabelNeighbors<true>(S, L, slot, pi, pos4, f);
-}
-template <typename F>
-__device__ __forceinline__ void forWaterNeighbors(const SceneDev& S, const NbrLists& L, int slot, float3 pi,
-                                                  const float4* __restrict__ pos4, F&& f) {
-    forLabelNeighbors<false>(S, L, slot, pi, pos4, f);
-}
-
-// Boundary particles within reach of slot, in stencil order.
-template <typename F>
-__device__ __forceinline__ void forBoundaryNeighbors(const SceneDev& S, const NbrLists& L, int slot, float3 pi,
-                                                     const float4* __restrict__ bpos4, F&& f) {
-    const int c = L.bcnt[slot];
-    if (c <= kMaxBNbr) {
-        const unsigned* __restrict__ p = L.bnbr + slot;
-#pragma unroll 1
-        for (int k = 0; k < c; ++k) f(int(p[size_t(k) * L.M]));
-    } else {
-        const int3 c = cellOf(S, pi);
-        const int z0 = max(c.z - 1, 0), z1 = min(c.z + 1, S.gz - 1) + 1;
-        for (int x = max(c.x - 1, 0); x <= min(c.x + 1, S.gx - 1); ++x)
-            for (int y = max(c.y - 1, 0); y <= min(c.y + 1, S.gy - 1); ++y) {
-                const int base = S.cell_off + (x * S.gy + y) * S.gz;
-                for (unsigned j = L.bcs[base + z0]; j < L.bcs[base + z1]; ++j)
-                    if (inReach(S, pi - xyz(bpos4[j]))) f(int(j));
-            }
-    }
-}
 
 // ---------------------------------------------------------------------- keys
 // Pos2GridHash (helper_thrust.cuh:66-89) into the global cell space; parking

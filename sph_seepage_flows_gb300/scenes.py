@@ -311,6 +311,63 @@ def adjoint_column(seed: int = 5) -> Scene:
                        sand_origin=(0.29, 0.02, 0.29), water_origin=(0.1, 0.02, 0.1))
 
 
+def capillary_rupture(r: float) -> float:
+    """Liquid-bridge rupture distance of two sand spheres of radius r
+    (ComputeDemCapillaryForces, cuda_dem_solver_common_gpu.cuh:63-65)."""
+    contact_angle = 30.0 / 180.0 * math.pi
+    vlb = 4.0 / 3.0 * math.pi * r ** 3 * 0.01 * 0.01
+    return (1.0 + 0.5 * contact_angle) * (vlb ** (1.0 / 3.0) + 0.1 * vlb ** (2.0 / 3.0))
+
+
+def adjoint_probe(seed: int = 11, sand_counts=(5, 3, 5), water_counts=(5, 6, 8), gap: float = 0.012,
+                  sand_velocity=(0.05, 0.0, 0.03), water_pitch: float = 0.019, water_speed: float = 0.01,
+                  margin: float = 5e-4) -> Scene:
+    """A small scene whose short-horizon trajectory stays away from the
+    model's value discontinuities, for gradient checks against finite
+    differences: sand at pitch 2r + s_rupture / 2 (every lattice pair inside
+    the liquid-bridge band, no sand-sand contact), its bottom layer pressed
+    1e-4 into the floor and sliding at sand_velocity (friction at the cap), a
+    slightly compressed water block (positive pressure) beside it at the
+    given gap, moving at random velocities up to water_speed (so no pair
+    sits on the viscosity switch dv . d = 0), no sand-water pair within margin
+    of h / 2 or h (the ends of the adhesion spline) and no sand whose nearest
+    water lies within margin of h (voidage onset)."""
+    r = 0.01
+    params = reference_params(sph_radius=r, dem_radius=r)
+    h = params.sph_kernel_radius
+    box = (0.36, 0.24, 0.36)
+    bparams = boundary_params((0.0, 0.0, 0.0), box, h)
+    sparams = solver_params()
+    rng = np.random.default_rng(seed)
+    srupt = capillary_rupture(r)
+    ps = 2.0 * r + 0.5 * srupt
+    sx, sy, sz = sand_counts
+    idx = np.stack(np.meshgrid(*[np.arange(c) for c in sand_counts], indexing="ij"), -1).reshape(-1, 3)
+    sand = np.array([0.20, 0.0199, 0.5 * box[2] - 0.5 * (sz - 1) * ps]) + idx * ps
+    sand = sand + rng.uniform(-0.1 * srupt, 0.1 * srupt, size=sand.shape) * np.array([1.0, 0.2, 1.0])
+    wx, wy, wz = water_counts
+    widx = np.stack(np.meshgrid(*[np.arange(c) for c in water_counts], indexing="ij"), -1).reshape(-1, 3)
+    wp = water_pitch
+    zc = 0.5 * box[2] - 0.5 * (wz - 1) * wp
+    water = np.array([0.20 - gap - (wx - 1) * wp, 0.035, zc]) + widx * wp
+    water = water + rng.uniform(-2e-4, 2e-4, size=water.shape)
+    wvel = rng.uniform(-water_speed, water_speed, size=water.shape)
+    # drop water in the singular windows of the adhesion spline
+    d = np.linalg.norm(water[:, None, :] - sand[None, :, :], axis=2)
+    bad = (np.abs(d - 0.5 * h) < margin).any(1) | (np.abs(d - h) < margin).any(1)
+    water = water[~bad]
+    wvel = wvel[~bad]
+    d = d[~bad]
+    nearest = d.min(0)
+    if np.any(np.abs(nearest - h) < margin):
+        raise ValueError("a sand particle's nearest water lies at the kernel radius; pick another seed")
+    sc = _assemble("adjoint_probe", params, bparams, sparams, sand.astype(np.float32), water.astype(np.float32),
+                   r, r, meta={"seed": seed, "sand_pitch": ps, "gap": gap})
+    sc.vel[: sand.shape[0]] = np.asarray(sand_velocity, dtype=np.float32)
+    sc.vel[sand.shape[0]:] = wvel.astype(np.float32)
+    return sc
+
+
 def remove_overlaps(scene: Scene, min_dist: float) -> Scene:
     """Drop water particles closer than min_dist to a sand particle (used
     where a water lattice is laid over a sand block)."""

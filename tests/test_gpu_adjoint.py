@@ -1,0 +1,164 @@
+"""Reverse-mode adjoint of the GPU substep (sf_adjoint_run) against FP64
+central finite differences of the oracle.
+
+Tolerance: each directional derivative and each parameter derivative is
+within 1e-3 relative of the FP64 finite difference (the gradient accuracy
+the adjoint is built to). The FD references are checked for convergence at
+two step sizes here and in test_adjoint_fd_cpu.py. Exact properties:
+checkpointing changes nothing (bit-identical results for checkpoint
+intervals 1, 3 and 8), the handle ends on the same state as
+sf_substeps_fixed, and a batched handle gives each scene the results of a
+single-scene handle. A torch.autograd.Function wrapping the C ABI checks
+that the gradients compose with autograd.
+"""
+
+import numpy as np
+import pytest
+
+from fd_oracle import (DT, PROBE_CASES, STEPS, checked_fd, directional_state, loss, param_derivative,
+                       probe_direction, probe_scene, probe_target)
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-3
+PARAMS = ("tan", "cap", "perm")
+
+
+def sim_of(scene):
+    from sph_seepage_flows_gb300.capi import Simulation
+    return Simulation(scene)
+
+
+@pytest.fixture(scope="module")
+def runs(cuda_lib):
+    out = {}
+    for seed, n_sub, damping in PROBE_CASES:
+        sc = probe_scene(seed, damping)
+        sim = sim_of(sc)
+        out[(seed, n_sub, damping)] = (sc, sim.adjoint(DT, n_sub, probe_target(sc), checkpoint_every=1))
+        sim.close()
+    return out
+
+
+@pytest.mark.parametrize("case", PROBE_CASES)
+def test_loss_matches_oracle(runs, oracle_mod, case):
+    sc, res = runs[case]
+    ref = loss(oracle_mod, sc, DT, case[1], probe_target(sc))
+    assert abs(res["loss"][0] - ref) <= 1e-4 * ref
+
+
+@pytest.mark.parametrize("case", PROBE_CASES)
+@pytest.mark.parametrize("which", ["pos", "vel"])
+def test_state_gradient_directional(runs, oracle_mod, case, which):
+    sc, res = runs[case]
+    u = probe_direction(sc, case[0])
+    fd = checked_fd(lambda h: directional_state(oracle_mod, sc, DT, case[1], probe_target(sc), which, u, h),
+                    STEPS[which], 1e-5)
+    g = res["grad_pos0" if which == "pos" else "grad_vel0"].astype(np.float64)
+    ad = float(np.sum(g * u))
+    assert abs(ad - fd) <= TOL * abs(fd), (ad, fd)
+
+
+@pytest.mark.parametrize("case", PROBE_CASES)
+@pytest.mark.parametrize("k", range(3))
+def test_parameter_gradient(runs, oracle_mod, case, k):
+    sc, res = runs[case]
+    fd = checked_fd(lambda h: param_derivative(oracle_mod, sc, DT, case[1], probe_target(sc), PARAMS[k], h),
+                    STEPS[PARAMS[k]], 1e-4)
+    ad = float(res["grad_params"][0, k])
+    assert abs(ad - fd) <= TOL * abs(fd), (PARAMS[k], ad, fd)
+
+
+def test_gradient_is_not_trivial(runs):
+    """Every tested derivative is well away from zero (the comparisons above
+    would pass vacuously otherwise)."""
+    sc, res = runs[PROBE_CASES[0]]
+    assert np.all(np.abs(res["grad_params"][0]) > 1e-12)
+    assert np.linalg.norm(res["grad_pos0"]) > 1e-3 and np.linalg.norm(res["grad_vel0"]) > 1e-7
+
+
+def test_checkpointing_is_exact(cuda_lib):
+    sc = probe_scene(11, 0.4)
+    target = probe_target(sc)
+    outs = []
+    for k in (1, 3, 8):
+        sim = sim_of(sc)
+        r = sim.adjoint(DT, 8, target, checkpoint_every=k)
+        r["final_pos"] = sim.field("pos", order="id")
+        r["final_vel"] = sim.field("vel", order="id")
+        outs.append(r)
+        sim.close()
+    for r in outs[1:]:
+        for key in ("loss", "grad_params", "grad_pos0", "grad_vel0", "final_pos", "final_vel"):
+            assert np.array_equal(r[key], outs[0][key]), key
+    sim = sim_of(sc)
+    sim.substeps_fixed(DT, 8)
+    assert np.array_equal(sim.field("pos", order="id"), outs[0]["final_pos"])
+    assert np.array_equal(sim.field("vel", order="id"), outs[0]["final_vel"])
+
+
+def test_batched_equals_single(cuda_lib):
+    from sph_seepage_flows_gb300.capi import Simulation
+    scs = [probe_scene(11, 0.4), probe_scene(12, 0.0)]
+    targets = [probe_target(s) for s in scs]
+    single = []
+    for s, t in zip(scs, targets):
+        sim = Simulation(s)
+        single.append(sim.adjoint(DT, 8, t))
+        sim.close()
+    sim = Simulation(scs)
+    both = sim.adjoint(DT, 8, np.concatenate(targets), checkpoint_every=4)
+    n0 = scs[0].n
+    for s, r in enumerate(single):
+        sl = slice(0, n0) if s == 0 else slice(n0, None)
+        assert both["loss"][s] == r["loss"][0]
+        assert np.array_equal(both["grad_params"][s], r["grad_params"][0])
+        assert np.array_equal(both["grad_pos0"][sl], r["grad_pos0"])
+        assert np.array_equal(both["grad_vel0"][sl], r["grad_vel0"])
+
+
+def test_argument_errors(cuda_lib):
+    from sph_seepage_flows_gb300.capi import SfError
+    sc = probe_scene(11, 0.4)
+    sim = sim_of(sc)
+    t = probe_target(sc)
+    for kw in ({"dt": 0.0, "n_substeps": 4}, {"dt": DT, "n_substeps": 0}):
+        with pytest.raises(SfError):
+            sim.adjoint(kw["dt"], kw["n_substeps"], t)
+    with pytest.raises(SfError):
+        sim.adjoint(DT, 4, t, checkpoint_every=0)
+    with pytest.raises(ValueError):
+        sim.adjoint(DT, 4, t[:-1])
+
+
+def test_autograd_function(cuda_lib):
+    """The C ABI wrapped as a torch.autograd.Function (test harness only):
+    backward of the loss returns the adjoint's gradients."""
+    torch = pytest.importorskip("torch")
+    sc = probe_scene(11, 0.4)
+
+    class Rollout(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, x0, v0, target):
+            s = probe_scene(11, 0.4)
+            s.pos = x0.detach().cpu().numpy().astype(np.float32)
+            s.vel = v0.detach().cpu().numpy().astype(np.float32)
+            sim = sim_of(s)
+            r = sim.adjoint(DT, 8, target.detach().cpu().numpy())
+            sim.close()
+            ctx.save_for_backward(torch.from_numpy(r["grad_pos0"]), torch.from_numpy(r["grad_vel0"]))
+            return torch.tensor(float(r["loss"][0]), dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx, g):
+            gx, gv = ctx.saved_tensors
+            return g * gx.double(), g * gv.double(), None
+
+    x0 = torch.tensor(sc.pos, dtype=torch.float64, requires_grad=True)
+    v0 = torch.tensor(sc.vel, dtype=torch.float64, requires_grad=True)
+    out = 3.0 * Rollout.apply(x0, v0, torch.tensor(probe_target(sc)))
+    out.backward()
+    sim = sim_of(sc)
+    r = sim.adjoint(DT, 8, probe_target(sc))
+    assert np.allclose(x0.grad.numpy(), 3.0 * r["grad_pos0"], rtol=1e-6, atol=0)
+    assert np.allclose(v0.grad.numpy(), 3.0 * r["grad_vel0"], rtol=1e-6, atol=0)
