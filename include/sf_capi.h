@@ -284,6 +284,30 @@ sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t che
                          const float* target_pos, float* loss_out, float* grad_params_out,
                          float* grad_pos0_out, float* grad_vel0_out, float* ms_out);
 
+/* Allocation-free cell sort (no counterpart in the reference; its neighbour
+ * searcher allocates its buffers in the CudaGNSearcher constructor).
+ *
+ * The sort stage of a single-scene handle without a handle and without any
+ * device allocation: cell keys of n positions (Pos2GridHash on `grid`), a
+ * stable radix sort and the cell-start table. Scratch lives in a static
+ * device array sized for at most SF_NOALLOC_MAX_PARTICLES particles
+ * (about 4.5 MB per device); larger n is rejected with SF_ERR_INVALID.
+ *   pos_dev             in:  n * 3 floats, device memory
+ *   perm_out_dev        out: n ints, device: perm[i] = input index of the
+ *                            i-th particle in cell order (stable)
+ *   cell_start_out_dev  out: G + 1 ints, device, G = grid cells:
+ *                            first sorted index with cell >= c; entry G = n
+ *   stream              the CUDA stream to use (NULL = the legacy default stream)
+ * The call waits for its stream before returning (it reads back a flag) and
+ * returns SF_ERR_DEVICE when a position is not finite. The first call on a
+ * device looks up the scratch address (cudaGetSymbolAddress), which may load
+ * the module: make the first call before any stream capture. Calls that
+ * overlap on the GPU (two streams or host threads) share the scratch and
+ * race: serialise them. Errors are reported by sf_last_error_string(NULL). */
+#define SF_NOALLOC_MAX_PARTICLES 262144
+sf_status sf_cell_sort_noalloc(const sf_boundary_params* grid, const float* pos_dev, int64_t n,
+                               int32_t* perm_out_dev, int32_t* cell_start_out_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -82,6 +82,8 @@ def load(path: str = LIB_PATH):
         "sf_set_tuning": (i32, [H, i32, i32]),
         "sf_last_error_string": (ctypes.c_char_p, [H]),
         "sf_adjoint_run": (i32, [H, f32, i64, i64, P(f32), P(f32), P(f32), P(f32), P(f32), P(f32)]),
+        "sf_cell_sort_noalloc": (i32, [P(SfBoundaryParams), ctypes.c_void_p, i64, ctypes.c_void_p, ctypes.c_void_p,
+                                       H]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

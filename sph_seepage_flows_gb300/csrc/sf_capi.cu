@@ -161,6 +161,11 @@ struct GraphCache {
 
 }  // namespace
 
+namespace sfg {
+// Error text of handle-less entry points (sf_last_error_string(NULL)).
+void setGlobalError(const std::string& msg) { g_createError = msg; }
+}  // namespace sfg
+
 struct sf_handle {
     cudaStream_t stream = nullptr;
     bool ownStream = false;
