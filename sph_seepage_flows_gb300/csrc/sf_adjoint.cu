@@ -17,11 +17,16 @@
 // which k is the neighbour of an output particle i. The latter are found by
 // walking k's own neighbour list (the lists are symmetric), so no
 // per-particle cotangent is written by two threads and no atomics are
-// needed; a pair term is evaluated once from each end. Pair Jacobians come
-// from forward-mode dual numbers (sf_dual.cuh) over the few inputs each pair
-// term has; the vector-Jacobian product is their contraction with the
-// output cotangent. Branch conditions (contact, friction cap, damping sign,
-// positive voidage, water clamp) are taken from the forward values.
+// needed. Pair terms that are antisymmetric (water pressure + viscosity:
+// a_j(j,k) = -(m_k / m_j) a_k(k,j); sand contacts: f_j(j,k) = -f_k(k,j))
+// are evaluated once per thread with the combined cotangent of both ends.
+//
+// The vector-Jacobian products of the SPH kernels and of the water, seepage,
+// boundary and sand-water terms are written out by hand below; the DEM +
+// capillary contact, the wall forces, the drag and the adhesion use
+// forward-mode dual numbers (sf_dual.cuh) over their few inputs. Branch
+// conditions (contact, friction cap, damping sign, positive voidage, water
+// clamp, viscosity switch) are taken from the forward values.
 //
 // Cotangents of positions and velocities between substeps are kept by
 // particle id (scene slot_off + id), so the sort needs no bookkeeping.
@@ -41,7 +46,123 @@ namespace sfg {
     const int sid = blockScene[(blockIdx.x * blockDim.x) / kSlotAlign];    \
     const SceneDev& S = scenes[sid];
 
-// ------------------------------------------------------- dual helpers
+// ------------------------------------------------------ neighbour cursors
+// The neighbours of one label (list, or the stencil when the list
+// overflowed) from a single call site, so that the loop body is inlined.
+template <bool kSand> struct LabelCursor {
+    const SceneDev* S;
+    const unsigned* cs;
+    const float4* pos4;
+    const unsigned* p;
+    long long step;
+    float3 pi;
+    int n, k, x, x1, y, y0, y1, z0, z1;
+    unsigned j, jEnd;
+    bool stencil;
+
+    __device__ __forceinline__ LabelCursor(const SceneDev& s, const NbrLists& L, int slot, float3 p_i,
+                                           const float4* __restrict__ pos)
+        : S(&s), cs(L.cs), pos4(pos), pi(p_i), k(0), j(0), jEnd(0) {
+        const unsigned c = L.cnt[slot];
+        stencil = int(c & 0xFFFFu) + int(c >> 16) > kMaxNbr;
+        n = kSand ? int(c & 0xFFFFu) : int(c >> 16);
+        p = L.nbr + slot + (kSand ? size_t(0) : size_t(kMaxNbr - 1) * size_t(L.M));
+        step = kSand ? L.M : -L.M;
+        x = x1 = y = y0 = y1 = z0 = z1 = 0;
+        if (stencil) {
+            const int3 cc = cellOf(s, p_i);
+            x = max(cc.x - 1, 0);
+            x1 = min(cc.x + 1, s.gx - 1);
+            y0 = max(cc.y - 1, 0);
+            y1 = min(cc.y + 1, s.gy - 1);
+            y = y0 - 1;
+            z0 = max(cc.z - 1, 0);
+            z1 = min(cc.z + 1, s.gz - 1) + 1;
+        }
+    }
+    __device__ __forceinline__ bool next(int& out) {
+        if (!stencil) {
+            if (k >= n) return false;
+            out = int(p[k * step]);
+            ++k;
+            return true;
+        }
+        for (;;) {
+            while (j < jEnd) {
+                const unsigned c = j++;
+                const float4 pj = pos4[c];
+                if ((kSand ? pj.w < 0.f : pj.w > 0.f) && inReach(*S, pi - xyz(pj))) {
+                    out = int(c);
+                    return true;
+                }
+            }
+            if (++y > y1) {
+                y = y0;
+                if (++x > x1) return false;
+            }
+            const int b = S->cell_off + (x * S->gy + y) * S->gz;
+            j = cs[b + z0];
+            jEnd = cs[b + z1];
+        }
+    }
+};
+
+// Boundary particles within reach (list, or the boundary stencil on overflow).
+struct BoundaryCursor {
+    const SceneDev* S;
+    const unsigned* bcs;
+    const float4* bpos4;
+    const unsigned* p;
+    long long M;
+    float3 pi;
+    int n, k, x, x1, y, y0, y1, z0, z1;
+    unsigned j, jEnd;
+    bool stencil;
+
+    __device__ __forceinline__ BoundaryCursor(const SceneDev& s, const NbrLists& L, int slot, float3 p_i,
+                                              const float4* __restrict__ bpos)
+        : S(&s), bcs(L.bcs), bpos4(bpos), p(L.bnbr + slot), M(L.M), pi(p_i), k(0), j(0), jEnd(0) {
+        n = L.bcnt[slot];
+        stencil = n > kMaxBNbr;
+        x = x1 = y = y0 = y1 = z0 = z1 = 0;
+        if (stencil) {
+            const int3 cc = cellOf(s, p_i);
+            x = max(cc.x - 1, 0);
+            x1 = min(cc.x + 1, s.gx - 1);
+            y0 = max(cc.y - 1, 0);
+            y1 = min(cc.y + 1, s.gy - 1);
+            y = y0 - 1;
+            z0 = max(cc.z - 1, 0);
+            z1 = min(cc.z + 1, s.gz - 1) + 1;
+        }
+    }
+    __device__ __forceinline__ bool next(int& out) {
+        if (!stencil) {
+            if (k >= n) return false;
+            out = int(p[size_t(k) * size_t(M)]);
+            ++k;
+            return true;
+        }
+        for (;;) {
+            while (j < jEnd) {
+                const unsigned c = j++;
+                if (inReach(*S, pi - xyz(bpos4[c]))) {
+                    out = int(c);
+                    return true;
+                }
+            }
+            if (++y > y1) {
+                y = y0;
+                if (++x > x1) return false;
+            }
+            const int b = S->cell_off + (x * S->gy + y) * S->gz;
+            j = bcs[b + z0];
+            jEnd = bcs[b + z1];
+        }
+    }
+};
+
+// ------------------------------------------------------- small helpers
 template <int K> __device__ __forceinline__ V3T<Dual<K>> dvec(float3 a, int k0) {
     return v3(dseed<K>(a.x, k0), dseed<K>(a.y, k0 + 1), dseed<K>(a.z, k0 + 2));
 }
@@ -55,8 +176,10 @@ template <int K> __device__ __forceinline__ float vjp(float3 u, const V3T<Dual<K
 template <int K> __device__ __forceinline__ float3 vjp3(float3 u, const V3T<Dual<K>>& o, int k0) {
     return mk3(vjp(u, o, k0), vjp(u, o, k0 + 1), vjp(u, o, k0 + 2));
 }
-template <int K> __device__ __forceinline__ float3 grad3(const Dual<K>& o, int k0) {
-    return mk3(o.d[k0], o.d[k0 + 1], o.d[k0 + 2]);
+__device__ __forceinline__ void operator-=(float3& a, float3 b) {
+    a.x -= b.x;
+    a.y -= b.y;
+    a.z -= b.z;
 }
 __device__ __forceinline__ void add3(float4& a, float3 b) {
     a.x += b.x;
@@ -83,71 +206,55 @@ __device__ __forceinline__ float2 blockSum2(float a, float b) {
     return s;  // valid in thread 0
 }
 
-// ----------------------------------------------------------- pair terms
-// The forward terms as templates on the scalar type (values identical to the
-// forward kernels in sf_kernels.cu; only their derivatives are used here).
+// ------------------------------------------- SPH kernels and their VJPs
+// Spiky gradient G(d) = phi(r) d (SpikyKernelGrad, cuda_sph_kernel.cuh:110-117)
+// and its symmetric Jacobian phi I + psi d d^T.
+struct SpikyD {
+    float3 g;
+    float phi, psi;
+};
+__device__ __forceinline__ SpikyD spikyD(const SceneDev& S, float3 d) {
+    SpikyD o;
+    const float r = len3(d);
+    if (r >= S.h || r < kEps) {
+        o.g = mk3(0.f, 0.f, 0.f);
+        o.phi = 0.f;
+        o.psi = 0.f;
+        return o;
+    }
+    const float hr = S.h - r;
+    o.phi = S.spiky * hr * hr / r;
+    o.g = o.phi * d;
+    o.psi = -S.spiky * hr * (S.h + r) / (r * r * r);
+    return o;
+}
+__device__ __forceinline__ float3 spikyVjp(const SpikyD& s, float3 d, float3 u) {
+    return s.phi * u + (s.psi * dot3(u, d)) * d;
+}
+// Gradient of the Poly6 kernel W(|d|) with respect to d.
+__device__ __forceinline__ float3 poly6Grad(const SceneDev& S, float3 d) {
+    const float r2 = dot3(d, d);
+    if (r2 >= S.h2) return mk3(0.f, 0.f, 0.f);
+    const float t = S.h2 - r2;
+    return (-6.f * S.poly6 * t * t) * d;
+}
+// Cotangents of P = p / max(eps, D^2), D = rho / max(eps, e) chained into (rho, p, e).
+__device__ __forceinline__ float3 chainPressureTerm(float Pbar, float Dbar, float p, float rho, float e) {
+    const float D = rho / fmaxf(kEps, e);
+    const float D2 = D * D;
+    const float pb = Pbar / fmaxf(kEps, D2);
+    if (D2 > kEps) Dbar += Pbar * (-2.f * p * D / (D2 * D2));
+    const float rb = Dbar / fmaxf(kEps, e);
+    const float eb = e > kEps ? Dbar * (-rho / (e * e)) : 0.f;
+    return mk3(rb, pb, eb);
+}
 
-// Pressure + artificial viscosity on water i from water j
-// (cuda_sph_sf_solver_gpu.cuh:343-406); d = x_i - x_j, dv = v_i - v_j.
-template <typename T>
-__device__ __forceinline__ V3T<T> waterPairT(const SceneDev& S, V3T<T> d, V3T<T> dv, T rhoI, T pI, T epsI, T rhoJ,
-                                             T pJ, T epsJ, float mj) {
-    const T di = rhoI / tmaxc(kEps, epsI);
-    const T dj = rhoJ / tmaxc(kEps, epsJ);
-    const V3T<T> nab = spikyGradT(S, d);
-    V3T<T> a = (-mj * (pI / tmaxc(kEps, di * di) + pJ / tmaxc(kEps, dj * dj))) * nab;
-    const T dd = dotT(dv, d);
-    if (val(dd) < 0.f) {
-        const T pij = (-S.nu / (di + dj)) * (dd / (dotT(d, d) + kEps));
-        a = a + (-mj * pij) * nab;
-    }
-    return a;
-}
-// Buoyancy + drag on water i from sand j (275-312); d = x_i - x_j.
-template <typename T>
-__device__ __forceinline__ V3T<T> seepageT(const SceneDev& S, V3T<T> d, T pI, T rhoI, T epsI, float rhoJ,
-                                           V3T<T> dragJ, float mj) {
-    const T di = rhoI / tmaxc(kEps, epsI);
-    const T wij = poly6T(S, lenT(d));
-    const V3T<T> nab = spikyGradT(S, d);
-    return (-mj * pI / tmaxc(kEps, di * rhoJ)) * nab + (-wij / di) * dragJ;
-}
-// Boundary pressure + viscosity on water i (cuda_sph_solver_common_gpu.cuh:
-// 89-139 with rho0 as the density); d = x_i - x_b.
-template <typename T>
-__device__ __forceinline__ V3T<T> boundaryT(const SceneDev& S, V3T<T> d, V3T<T> vI, T pI, float vol) {
-    const V3T<T> nab = spikyGradT(S, d);
-    V3T<T> a = (-S.rho0 * vol * (pI / fmaxf(kEps, S.rho0 * S.rho0))) * nab;
-    const T dd = dotT(vI, d);
-    if (val(dd) < 0.f) {
-        const T pij = (-S.bnu / (2.f * S.rho0)) * (dd / (dotT(d, d) + kEps));
-        a = a + (-vol * S.rho0 * pij) * nab;
-    }
-    return a;
-}
+// ------------------------------------------ dual-number pair terms
 // DEM + capillary force on sand i from sand j (21-50, 83-109); d = x_j - x_i, dv = v_j - v_i.
 template <typename T>
 __device__ __forceinline__ V3T<T> contactT(const SceneDev& S, V3T<T> d, V3T<T> dv, T satI, T satJ, T tanPhi,
                                            T capScale) {
     return demForceT(d, dv, S.rij2, S.kn, S.ks, tanPhi * tanPhi) + capillaryForceT(S, d, (satI + satJ) / 2.f, capScale);
-}
-// Buoyancy + adhesion on sand i from water j (240-273, 314-341); d = x_i - x_j.
-template <typename T>
-__device__ __forceinline__ V3T<T> sandWaterT(const SceneDev& S, V3T<T> d, float mi, float rhoI, T pJ, T rhoJ, T epsJ,
-                                             V3T<T> avgAdhJ, float mj) {
-    const T wij = poly6T(S, lenT(d));
-    V3T<T> f = d * 0.f;
-    if (val(epsJ) > 0.f && val(epsJ) <= 1.f) {
-        const T dj = rhoJ / tmaxc(kEps, epsJ);
-        f = (-mi * mj * pJ / tmaxc(kEps, rhoI * dj)) * spikyGradT(S, d);
-    }
-    return f + (wij * (mi / fmaxf(kEps, rhoI))) * avgAdhJ;
-}
-// Water j's term of v_w of sand i; d = x_i - x_j.
-template <typename T>
-__device__ __forceinline__ T vwTermT(const SceneDev& S, V3T<T> d, T rhoJ, T epsJ, float mj) {
-    if (!(val(epsJ) > 0.f && val(epsJ) <= 1.f)) return lenT(d) * 0.f;
-    return (mj / (rhoJ / tmaxc(kEps, epsJ))) * poly6T(S, lenT(d));
 }
 // ComputeDemWorldBoundaryForces on sand i (cuda_dem_solver_common_gpu.cuh:132-199).
 template <typename T>
@@ -179,10 +286,6 @@ template <typename T>
 __device__ __forceinline__ V3T<T> adhesionT(const SceneDev& S, V3T<T> d, T satJ, float mi, float mj) {
     const T l = lenT(d);
     return (bezierT(S.adhG, satJ, 1.f) * mi * mj * adhesionSplineT(S, l)) * d / tmaxc(kEps, l);
-}
-// Gradient of W(|d|) with respect to d.
-__device__ __forceinline__ float3 poly6Grad(const SceneDev& S, float3 d) {
-    return grad3(poly6T(S, lenT(dvec<3>(d, 0))), 0);
 }
 
 // ------------------------------------------------------------- kernels
@@ -245,7 +348,12 @@ __global__ void kAdjIntegrate(const SceneDev* __restrict__ scenes, const int* __
     A.drag[slot] = z;
 }
 
-// A2: water momentum (acc = g + a - F_adh / m).
+// A2: water momentum (ComputeSFWaterLinearMomentum_CUDA, acc = g + a - F_adh / m).
+// Water pair term of particle k from water j, d = x_k - x_j, dv = v_k - v_j:
+//   a_k(k,j) = m_j T,  a_j(j,k) = -m_k T,
+//   T = -(P_k + P_j) G(d) - [dv.d < 0] Pi G(d),  Pi = kappa dv.d / (d.d + eps),
+//   kappa = -nu / (D_k + D_j),  D = rho / max(eps, e),  P = p / max(eps, D^2),
+// so both ends are served by the cotangent c = m_j a-bar_k - m_k a-bar_j on T.
 __global__ void __launch_bounds__(kSlotAlign) kAdjWater(const SceneDev* __restrict__ scenes,
                                                         const int* __restrict__ blockScene, AdjBuffers A,
                                                         PassBuffers b) {
@@ -253,81 +361,110 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjWater(const SceneDev* __restri
     const float4 pk4 = b.pos4[slot];
     if (pk4.w == 0.f) return;
     const NbrLists& L = b.lists;
-    const float3 xk = xyz(pk4), vk = xyz(b.vel4[slot]);
-    const float rhoK = b.vel4[slot].w, pK = b.aux4[slot].x, epsK = b.aux4[slot].w;
+    const float3 xk = xyz(pk4);
+    const float4 vk4 = b.vel4[slot];
+    const float3 vk = xyz(vk4);
+    const float rhoK = vk4.w, pK = b.aux4[slot].x, epsK = b.aux4[slot].w;
     float3 gx = mk3(0.f, 0.f, 0.f), gv = gx;
-    float grho = 0.f, gp = 0.f, geps = 0.f;
     if (pk4.w > 0.f) {
         const float mk = pk4.w;
         const float3 ak = xyz(A.acc[slot]);
         A.adh[slot] = f4(ak / -mk);
-        forWaterNeighbors(S, L, slot, xk, b.pos4, [&](int j) {
-            if (j == slot) return;
+        const float Dk = rhoK / fmaxf(kEps, epsK);
+        const float Pk = pK / fmaxf(kEps, Dk * Dk);
+        float Pbar = 0.f, Dbar = 0.f, pbar = 0.f;
+        LabelCursor<false> wc(S, L, slot, xk, b.pos4);
+        for (int j; wc.next(j);) {
+            if (j == slot) continue;
             const float4 pj4 = b.pos4[j];
-            const float3 xj = xyz(pj4), vj = xyz(b.vel4[j]);
-            const float rhoJ = b.vel4[j].w, pJ = b.aux4[j].x, epsJ = b.aux4[j].w;
-            {   // own term a_k(k, j); seeds d 0-2, dv 3-5, rho_k 6, p_k 7, eps_k 8
-                const auto o = waterPairT<Dual<9>>(S, dvec<9>(xk - xj, 0), dvec<9>(vk - vj, 3), dseed<9>(rhoK, 6),
-                                                   dseed<9>(pK, 7), dseed<9>(epsK, 8), dconst<9>(rhoJ),
-                                                   dconst<9>(pJ), dconst<9>(epsJ), pj4.w);
-                gx += vjp3(ak, o, 0);
-                gv += vjp3(ak, o, 3);
-                grho += vjp(ak, o, 6);
-                gp += vjp(ak, o, 7);
-                geps += vjp(ak, o, 8);
+            const float3 d = xk - xyz(pj4);
+            const SpikyD sp = spikyD(S, d);
+            if (sp.phi == 0.f && sp.psi == 0.f) continue;
+            const float4 vj4 = b.vel4[j];
+            const float4 aj4 = b.aux4[j];
+            const float Dj = vj4.w / fmaxf(kEps, aj4.w);
+            const float Pj = aj4.x / fmaxf(kEps, Dj * Dj);
+            const float3 c = pj4.w * ak - mk * xyz(A.acc[j]);
+            const float cg = dot3(c, sp.g);
+            float coef = -(Pk + Pj);
+            Pbar -= cg;
+            const float3 dv = vk - xyz(vj4);
+            const float dd = dot3(dv, d);
+            if (dd < 0.f) {
+                const float q = dot3(d, d) + kEps;
+                const float sD = Dk + Dj;
+                const float kappa = -S.nu / sD;
+                coef -= kappa * (dd / q);
+                gx += (-cg * kappa) * (dv / q - (2.f * dd / (q * q)) * d);
+                gv += (-cg * kappa / q) * d;
+                Dbar += cg * (-(dd / q) * S.nu / (sD * sD));
             }
-            {   // k as the neighbour in a_j(j, k): d = x_j - x_k, dv = v_j - v_k
-                const float3 aj = xyz(A.acc[j]);
-                const auto o = waterPairT<Dual<9>>(S, dvec<9>(xj - xk, 0), dvec<9>(vj - vk, 3), dconst<9>(rhoJ),
-                                                   dconst<9>(pJ), dconst<9>(epsJ), dseed<9>(rhoK, 6),
-                                                   dseed<9>(pK, 7), dseed<9>(epsK, 8), mk);
-                gx += -vjp3(aj, o, 0);
-                gv += -vjp3(aj, o, 3);
-                grho += vjp(aj, o, 6);
-                gp += vjp(aj, o, 7);
-                geps += vjp(aj, o, 8);
-            }
-        });
-        forSandNeighbors(S, L, slot, xk, b.pos4, [&](int j) {
+            gx += coef * spikyVjp(sp, d, c);
+        }
+        // seepage terms of sand j: (-m_j p_k / max(eps, D_k rho_j)) G(d) - W(d) / D_k drag_j
+        LabelCursor<true> sc(S, L, slot, xk, b.pos4);
+        for (int j; sc.next(j);) {
             const float4 pj4 = b.pos4[j];
-            // seeds d 0-2, p_k 3, rho_k 4, eps_k 5
-            const auto o = seepageT<Dual<6>>(S, dvec<6>(xk - xyz(pj4), 0), dseed<6>(pK, 3), dseed<6>(rhoK, 4),
-                                             dseed<6>(epsK, 5), b.vel4[j].w, dvecc<6>(xyz(b.drag4[j])), -pj4.w);
-            gx += vjp3(ak, o, 0);
-            gp += vjp(ak, o, 3);
-            grho += vjp(ak, o, 4);
-            geps += vjp(ak, o, 5);
-        });
-        forBoundaryNeighbors(S, L, slot, xk, b.bpos4, [&](int bb) {
+            const float3 d = xk - xyz(pj4);
+            const SpikyD sp = spikyD(S, d);
+            const float mj = -pj4.w, rhoJ = b.vel4[j].w;
+            const float3 dragJ = xyz(b.drag4[j]);
+            const float den = Dk * rhoJ;
+            const float ug = dot3(ak, sp.g), ud = dot3(ak, dragJ);
+            gx += (-mj * pK / fmaxf(kEps, den)) * spikyVjp(sp, d, ak) + (-ud / Dk) * poly6Grad(S, d);
+            pbar += ug * (-mj / fmaxf(kEps, den));
+            if (den > kEps) Dbar += ug * (mj * pK * rhoJ / (den * den));
+            Dbar += ud * poly6(S, len3(d)) / (Dk * Dk);
+        }
+        // boundary pressure and viscosity (rho0 as the density)
+        const float gam0 = -S.rho0 / fmaxf(kEps, S.rho0 * S.rho0);
+        const float kb = -S.bnu / (2.f * S.rho0);
+        BoundaryCursor bc(S, L, slot, xk, b.bpos4);
+        for (int bb; bc.next(bb);) {
             const float4 bj = b.bpos4[bb];
-            const auto o = boundaryT<Dual<7>>(S, dvec<7>(xk - xyz(bj), 0), dvec<7>(vk, 3), dseed<7>(pK, 6), fabsf(bj.w));
-            gx += vjp3(ak, o, 0);
-            gv += vjp3(ak, o, 3);
-            gp += vjp(ak, o, 6);
-        });
+            const float vol = fabsf(bj.w);
+            const float3 d = xk - xyz(bj);
+            const SpikyD sp = spikyD(S, d);
+            const float ug = dot3(ak, sp.g);
+            const float gam = gam0 * vol;
+            pbar += gam * ug;
+            float coef = gam * pK;
+            const float dd = dot3(vk, d);
+            if (dd < 0.f) {
+                const float q = dot3(d, d) + kEps;
+                const float w = -vol * S.rho0 * kb;
+                coef += w * (dd / q);
+                gx += (ug * w) * (vk / q - (2.f * dd / (q * q)) * d);
+                gv += (ug * w / q) * d;
+            }
+            gx += coef * spikyVjp(sp, d, ak);
+        }
+        const float3 s3 = chainPressureTerm(Pbar, Dbar, pK, rhoK, epsK);
+        float4 s = A.s[slot];
+        s.x += s3.x;
+        s.y += s3.y + pbar;
+        s.z += s3.z;
+        A.s[slot] = s;
     } else {
-        // sand k in the seepage term of water i: d = x_i - x_k; seeds d 0-2, drag_k 3-5
+        // sand k in the seepage term of water i: d = x_i - x_k
         const float mk = -pk4.w;
         const float3 dragK = xyz(b.drag4[slot]);
         float3 gdrag = mk3(0.f, 0.f, 0.f);
-        forWaterNeighbors(S, L, slot, xk, b.pos4, [&](int i) {
+        LabelCursor<false> wc(S, L, slot, xk, b.pos4);
+        for (int i; wc.next(i);) {
             const float4 pi4 = b.pos4[i];
+            const float3 d = xyz(pi4) - xk;
+            const SpikyD sp = spikyD(S, d);
+            const float Di = b.vel4[i].w / fmaxf(kEps, b.aux4[i].w);
             const float3 ai = xyz(A.acc[i]);
-            const auto o = seepageT<Dual<6>>(S, dvec<6>(xyz(pi4) - xk, 0), dconst<6>(b.aux4[i].x),
-                                             dconst<6>(b.vel4[i].w), dconst<6>(b.aux4[i].w), rhoK,
-                                             dvec<6>(dragK, 3), mk);
-            gx += -vjp3(ai, o, 0);
-            gdrag += vjp3(ai, o, 3);
-        });
+            const float alpha = -mk * b.aux4[i].x / fmaxf(kEps, Di * rhoK);
+            gx -= alpha * spikyVjp(sp, d, ai) + (-dot3(ai, dragK) / Di) * poly6Grad(S, d);
+            gdrag += (-poly6(S, len3(d)) / Di) * ai;
+        }
         A.drag[slot] = f4(gdrag);
     }
     add3(A.x[slot], gx);
     add3(A.v[slot], gv);
-    float4 s = A.s[slot];
-    s.x += grho;
-    s.y += gp;
-    s.z += geps;
-    A.s[slot] = s;
 }
 
 // A3a: per sand particle: v_w, drag, walls and shape-boundary DEM; writes
@@ -344,11 +481,12 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjSandSelf(const SceneDev* __res
         const float rhoK = b.vel4[slot].w, epsK = b.aux4[slot].w;
         const float tanPhi = sqrtf(S.tan2);
         float vw = 0.f;
-        forWaterNeighbors(S, b.lists, slot, xk, b.pos4, [&](int j) {
+        LabelCursor<false> wc(S, b.lists, slot, xk, b.pos4);
+        for (int j; wc.next(j);) {
             const float4 pj4 = b.pos4[j];
-            const float3 d = xk - xyz(pj4);
-            vw += vwTermT<float>(S, v3(d.x, d.y, d.z), b.vel4[j].w, b.aux4[j].w, pj4.w);
-        });
+            const float ej = b.aux4[j].w;
+            if (ej > 0.f && ej <= 1.f) vw += pj4.w / (b.vel4[j].w / fmaxf(kEps, ej)) * poly6(S, len3(xk - xyz(pj4)));
+        }
         const float3 fb = (2.f / mk) * xyz(A.acc[slot]);
         const float3 dragB = xyz(A.drag[slot]);
         // df; seeds eps 0, flow 1-3, v 4-6, permeability scale 7
@@ -361,9 +499,7 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjSandSelf(const SceneDev* __res
             dfb = dfb + dragB / vw;
             vwb = -dot3(dragB, mk3(df.x.v, df.y.v, df.z.v)) / (vw * vw);
         }
-        float4 s = A.s[slot];
-        s.z += vjp(dfb, df, 0);
-        A.s[slot] = s;
+        A.s[slot].z += vjp(dfb, df, 0);
         A.flow[slot] = f4(vjp3(dfb, df, 1));
         float3 gv = vjp3(dfb, df, 4);
         gPerm = vjp(dfb, df, 7);
@@ -373,15 +509,16 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjSandSelf(const SceneDev* __res
         gv += vjp3(fb, w, 3);
         gTan = vjp(fb, w, 6);
         if (S.shape_boundary) {
-            forBoundaryNeighbors(S, b.lists, slot, xk, b.bpos4, [&](int bb) {
+            BoundaryCursor bc(S, b.lists, slot, xk, b.bpos4);
+            for (int bb; bc.next(bb);) {
                 const float4 bj = b.bpos4[bb];
-                if (!(bj.w < 0.f)) return;
+                if (!(bj.w < 0.f)) continue;
                 const auto tp = dseed<7>(tanPhi, 6);
                 const auto o = demForceT(dvec<7>(xk - xyz(bj), 0), -dvec<7>(vk, 3), S.rij2, S.kn, S.ks, tp * tp);
                 gx += vjp3(fb, o, 0);
                 gv += vjp3(fb, o, 3);
                 gTan += vjp(fb, o, 6);
-            });
+            }
         }
         add3(A.x[slot], gx);
         add3(A.v[slot], gv);
@@ -394,7 +531,11 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjSandSelf(const SceneDev* __res
     }
 }
 
-// A3b: sand pair terms (contacts, buoyancy + adhesion, v_w) from both ends.
+// A3b: sand pair terms. Contacts (one dual evaluation per pair serves both
+// ends: f_j(j,k) = -f_k(k,j)); buoyancy + adhesion and v_w with water, from
+// the sand end and from the water end:
+//   f_i += [0 < e_j <= 1] (-m_i m_j p_j / max(eps, rho_i D_j)) G(x_i - x_j) + W vol_i avgadh_j,
+//   v_w,i += [0 < e_j <= 1] (m_j / D_j) W(x_i - x_j).
 __global__ void __launch_bounds__(kSlotAlign) kAdjSandPairs(const SceneDev* __restrict__ scenes,
                                                             const int* __restrict__ blockScene, AdjBuffers A,
                                                             PassBuffers b, float* __restrict__ paramPartial) {
@@ -402,86 +543,100 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjSandPairs(const SceneDev* __re
     const float4 pk4 = b.pos4[slot];
     float gTan = 0.f, gCap = 0.f;
     if (pk4.w != 0.f) {
-        const float3 xk = xyz(pk4), vk = xyz(b.vel4[slot]);
-        const float rhoK = b.vel4[slot].w, pK = b.aux4[slot].x, satK = b.aux4[slot].z, epsK = b.aux4[slot].w;
-        float3 gx = mk3(0.f, 0.f, 0.f), gv = gx, gadh = gx;
-        float gsat = 0.f, grho = 0.f, gp = 0.f, geps = 0.f;
+        const NbrLists& L = b.lists;
+        const float3 xk = xyz(pk4);
+        const float4 vk4 = b.vel4[slot];
+        const float3 vk = xyz(vk4);
+        const float4 ak4 = b.aux4[slot];
+        const float rhoK = vk4.w, pK = ak4.x, satK = ak4.z, epsK = ak4.w;
+        float3 gx = mk3(0.f, 0.f, 0.f), gv = gx;
         if (pk4.w < 0.f) {
             const float mk = -pk4.w;
             const float4 fk4 = A.f[slot];
             const float3 fb = xyz(fk4);
-            const float tanPhi = sqrtf(S.tan2);
-            forSandNeighbors(S, b.lists, slot, xk, b.pos4, [&](int j) {
-                if (j == slot) return;
-                const float4 pj4 = b.pos4[j];
-                const float3 d = xyz(pj4) - xk;
-                if (!(dot3(d, d) < S.dem_reach2)) return;
-                const float3 vj = xyz(b.vel4[j]);
-                const float satJ = b.aux4[j].z;
-                {   // own f_k(k, j), d = x_j - x_k; seeds d 0-2, dv 3-5, sat_k 6, tan phi 7, capillary scale 8
-                    const auto o = contactT<Dual<9>>(S, dvec<9>(d, 0), dvec<9>(vj - vk, 3), dseed<9>(satK, 6),
-                                                     dconst<9>(satJ), dseed<9>(tanPhi, 7), dseed<9>(1.f, 8));
-                    gx += -vjp3(fb, o, 0);
-                    gv += -vjp3(fb, o, 3);
-                    gsat += vjp(fb, o, 6);
-                    gTan += vjp(fb, o, 7);
-                    gCap += vjp(fb, o, 8);
-                }
-                {   // k as the neighbour in f_j(j, k), d = x_k - x_j; seeds d 0-2, dv 3-5, sat_k 6
-                    const float3 fj = xyz(A.f[j]);
-                    const auto o = contactT<Dual<7>>(S, dvec<7>(-1.f * d, 0), dvec<7>(vk - vj, 3), dconst<7>(satJ),
-                                                     dseed<7>(satK, 6), dconst<7>(tanPhi), dconst<7>(1.f));
-                    gx += vjp3(fj, o, 0);
-                    gv += vjp3(fj, o, 3);
-                    gsat += vjp(fj, o, 6);
-                }
-            });
             const float vwb = fk4.w;
-            forWaterNeighbors(S, b.lists, slot, xk, b.pos4, [&](int j) {
+            const float tanPhi = sqrtf(S.tan2);
+            float gsat = 0.f;
+            // contacts: the contact list, or the sand list filtered by the DEM reach
+            const int ncon = L.ccnt[slot];
+            const bool filtered = ncon > kMaxContact;
+            LabelCursor<true> sc(S, L, slot, xk, b.pos4);
+            for (int k = 0;; ++k) {
+                int j;
+                if (!filtered) {
+                    if (k >= ncon) break;
+                    j = int(L.cnbr[slot + size_t(k) * size_t(L.M)]);
+                } else {
+                    if (!sc.next(j)) break;
+                    if (j == slot) continue;
+                    const float3 dd = xyz(b.pos4[j]) - xk;
+                    if (!(dot3(dd, dd) < S.dem_reach2)) continue;
+                }
+                const float3 d = xyz(b.pos4[j]) - xk;
+                const float3 c = fb - xyz(A.f[j]);
+                // seeds d 0-2, dv 3-5, sat_k 6, tan phi 7, capillary scale 8
+                const auto o = contactT<Dual<9>>(S, dvec<9>(d, 0), dvec<9>(xyz(b.vel4[j]) - vk, 3), dseed<9>(satK, 6),
+                                                 dconst<9>(b.aux4[j].z), dseed<9>(tanPhi, 7), dseed<9>(1.f, 8));
+                gx -= vjp3(c, o, 0);
+                gv -= vjp3(c, o, 3);
+                gsat += vjp(c, o, 6);
+                gTan += vjp(fb, o, 7);
+                gCap += vjp(fb, o, 8);
+            }
+            const float volK = mk / fmaxf(kEps, rhoK);
+            LabelCursor<false> wc(S, L, slot, xk, b.pos4);
+            for (int j; wc.next(j);) {
                 const float4 pj4 = b.pos4[j];
                 const float3 d = xk - xyz(pj4);
-                const float rhoJ = b.vel4[j].w, epsJ = b.aux4[j].w;
-                const auto o = sandWaterT<Dual<3>>(S, dvec<3>(d, 0), mk, rhoK, dconst<3>(b.aux4[j].x),
-                                                   dconst<3>(rhoJ), dconst<3>(epsJ), dvecc<3>(xyz(b.avgadh4[j])),
-                                                   pj4.w);
-                gx += vjp3(fb, o, 0);
-                if (vwb != 0.f)
-                    gx += vwb * grad3(vwTermT<Dual<3>>(S, dvec<3>(d, 0), dconst<3>(rhoJ), dconst<3>(epsJ), pj4.w), 0);
-            });
+                const float3 gW = poly6Grad(S, d);
+                gx += (volK * dot3(fb, xyz(b.avgadh4[j]))) * gW;
+                const float ej = b.aux4[j].w;
+                if (ej > 0.f && ej <= 1.f) {
+                    const float Dj = b.vel4[j].w / fmaxf(kEps, ej);
+                    const float sigma = -mk * pj4.w * b.aux4[j].x / fmaxf(kEps, rhoK * Dj);
+                    gx += sigma * spikyVjp(spikyD(S, d), d, fb) + (vwb * pj4.w / Dj) * gW;
+                }
+            }
+            A.s[slot].w += gsat;
         } else {
-            // water k in the buoyancy / adhesion and v_w terms of sand i: d = x_i - x_k
+            // water k in the terms of sand i: d = x_i - x_k
             const float mk = pk4.w;
             const float3 avgAdhK = xyz(b.avgadh4[slot]);
-            forSandNeighbors(S, b.lists, slot, xk, b.pos4, [&](int i) {
+            const bool inBand = epsK > 0.f && epsK <= 1.f;
+            const float Dk = rhoK / fmaxf(kEps, epsK);
+            float3 gadh = mk3(0.f, 0.f, 0.f);
+            float pbar = 0.f, Dbar = 0.f;
+            LabelCursor<true> sc(S, L, slot, xk, b.pos4);
+            for (int i; sc.next(i);) {
                 const float4 pi4 = b.pos4[i];
                 const float4 fi4 = A.f[i];
-                const float3 d = xyz(pi4) - xk;
-                // seeds d 0-2, p_k 3, rho_k 4, eps_k 5, avg adhesion_k 6-8
-                const auto o = sandWaterT<Dual<9>>(S, dvec<9>(d, 0), -pi4.w, b.vel4[i].w, dseed<9>(pK, 3),
-                                                   dseed<9>(rhoK, 4), dseed<9>(epsK, 5), dvec<9>(avgAdhK, 6), mk);
                 const float3 fi = xyz(fi4);
-                gx += -vjp3(fi, o, 0);
-                gp += vjp(fi, o, 3);
-                grho += vjp(fi, o, 4);
-                geps += vjp(fi, o, 5);
-                gadh += vjp3(fi, o, 6);
-                if (fi4.w != 0.f) {  // seeds d 0-2, rho_k 3, eps_k 4
-                    const auto t = vwTermT<Dual<5>>(S, dvec<5>(d, 0), dseed<5>(rhoK, 3), dseed<5>(epsK, 4), mk);
-                    gx += -fi4.w * grad3(t, 0);
-                    grho += fi4.w * t.d[3];
-                    geps += fi4.w * t.d[4];
+                const float3 d = xyz(pi4) - xk;
+                const float mi = -pi4.w, rhoI = b.vel4[i].w;
+                const float volI = mi / fmaxf(kEps, rhoI);
+                const float W = poly6(S, len3(d));
+                const float3 gW = poly6Grad(S, d);
+                gadh += (W * volI) * fi;
+                gx -= (volI * dot3(fi, avgAdhK)) * gW;
+                if (inBand) {
+                    const float den = rhoI * Dk;
+                    const SpikyD sp = spikyD(S, d);
+                    const float ug = dot3(fi, sp.g);
+                    gx -= (-mi * mk * pK / fmaxf(kEps, den)) * spikyVjp(sp, d, fi) + (fi4.w * mk / Dk) * gW;
+                    pbar += ug * (-mi * mk / fmaxf(kEps, den));
+                    if (den > kEps) Dbar += ug * (mi * mk * pK * rhoI / (den * den));
+                    Dbar += fi4.w * (-mk * W / (Dk * Dk));
                 }
-            });
+            }
+            add3(A.avgadh[slot], gadh);
+            float4 s = A.s[slot];
+            s.x += Dbar / fmaxf(kEps, epsK);
+            s.y += pbar;
+            if (epsK > kEps) s.z += Dbar * (-rhoK / (epsK * epsK));
+            A.s[slot] = s;
         }
         add3(A.x[slot], gx);
         add3(A.v[slot], gv);
-        add3(A.avgadh[slot], gadh);
-        float4 s = A.s[slot];
-        s.x += grho;
-        s.y += gp;
-        s.z += geps;
-        s.w += gsat;
-        A.s[slot] = s;
     }
     const float2 t = blockSum2(gTan, gCap);
     if (threadIdx.x == 0) {
@@ -501,22 +656,24 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjVoidSelf(const SceneDev* __res
     const float3 xk = xyz(pk4);
     if (pk4.w < 0.f) {
         float num = 0.f, den = 0.f;
-        forWaterNeighbors(S, b.lists, slot, xk, b.pos4, [&](int j) {
+        LabelCursor<false> wc(S, b.lists, slot, xk, b.pos4);
+        for (int j; wc.next(j);) {
             const float4 pj4 = b.pos4[j];
             const float vj = pj4.w / b.vel4[j].w;
             const float wij = poly6(S, len3(xk - xyz(pj4)));
             num += b.aux4[j].y * vj * wij;
             den += vj * wij;
-        });
+        }
         const float eb = A.s[slot].z;
         A.r[slot] = den != 0.f ? make_float4(eb / den, -eb * num / (den * den), 0.f, 0.f)
                                : make_float4(0.f, 0.f, 0.f, 0.f);
     } else {
         float vs = 0.f;
-        forSandNeighbors(S, b.lists, slot, xk, b.pos4, [&](int j) {
+        LabelCursor<true> sc(S, b.lists, slot, xk, b.pos4);
+        for (int j; sc.next(j);) {
             const float4 pj4 = b.pos4[j];
             vs += -pj4.w / b.vel4[j].w * poly6(S, len3(xk - xyz(pj4)));
-        });
+        }
         const float3 avgB = xyz(A.avgadh[slot]);
         float3 tot = xyz(A.adh[slot]);
         float vsb = 0.f;
@@ -538,51 +695,59 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjVoidPairs(const SceneDev* __re
     const float3 xk = xyz(pk4);
     const float rhoK = b.vel4[slot].w;
     float3 gx = mk3(0.f, 0.f, 0.f);
-    float gsat = 0.f, grho = 0.f, geps = 0.f;
     if (pk4.w < 0.f) {
         const float mk = -pk4.w;
         const float4 rk = A.r[slot];
         const float satK = b.aux4[slot].z;
         const float vk = mk / rhoK;
-        forWaterNeighbors(S, b.lists, slot, xk, b.pos4, [&](int j) {
+        float gsat = 0.f;
+        LabelCursor<false> wc(S, b.lists, slot, xk, b.pos4);
+        for (int j; wc.next(j);) {
             const float4 pj4 = b.pos4[j];
-            // own num / den sums: d = x_k - x_j
+            const float3 d = xyz(pj4) - xk;  // x_j - x_k
+            const float3 gW = poly6Grad(S, d);
+            // own num / den sums over W(x_k - x_j): gradient -gW
             const float vj = pj4.w / b.vel4[j].w;
-            gx += (rk.x * b.aux4[j].y * vj + rk.y * vj) * poly6Grad(S, xk - xyz(pj4));
-            // k in the adhesion and v_s of water j: d = x_j - x_k; seeds d 0-2, sat_k 3
+            gx -= (rk.x * b.aux4[j].y * vj + rk.y * vj) * gW;
+            // k in the adhesion and v_s of water j; seeds d 0-2, sat_k 3
             const float4 rj = A.r[j];
-            const float3 d = xyz(pj4) - xk;
-            const auto o = adhesionT<Dual<4>>(S, dvec<4>(d, 0), dseed<4>(satK, 3), pj4.w, mk);
-            gx += -vjp3(xyz(rj), o, 0);
-            gsat += vjp(xyz(rj), o, 3);
-            if (rj.w != 0.f) gx += (-rj.w * vk) * poly6Grad(S, d);
-        });
+            if (2.f * dot3(d, d) > 0.5f * S.h2) {  // the adhesion spline vanishes for |d| <= h / 2
+                const auto o = adhesionT<Dual<4>>(S, dvec<4>(d, 0), dseed<4>(satK, 3), pj4.w, mk);
+                gx -= vjp3(xyz(rj), o, 0);
+                gsat += vjp(xyz(rj), o, 3);
+            }
+            gx -= (rj.w * vk) * gW;
+        }
+        A.s[slot].w += gsat;
     } else {
         const float mk = pk4.w;
         const float4 rk = A.r[slot];
         const float epsfK = b.aux4[slot].y;
-        forSandNeighbors(S, b.lists, slot, xk, b.pos4, [&](int j) {
+        float grho = 0.f, geps = 0.f;
+        LabelCursor<true> sc(S, b.lists, slot, xk, b.pos4);
+        for (int j; sc.next(j);) {
             const float4 pj4 = b.pos4[j];
             const float3 d = xk - xyz(pj4);
+            const float3 gW = poly6Grad(S, d);
             // own adhesion and v_s terms
-            gx += vjp3(xyz(rk), adhesionT<Dual<3>>(S, dvec<3>(d, 0), dconst<3>(b.aux4[j].z), mk, -pj4.w), 0);
-            if (rk.w != 0.f) gx += (rk.w * (-pj4.w / b.vel4[j].w)) * poly6Grad(S, d);
-            // k in the num / den of sand j: d = x_j - x_k; seeds d 0-2, eps_f,k 3, rho_k 4
+            if (2.f * dot3(d, d) > 0.5f * S.h2)
+                gx += vjp3(xyz(rk), adhesionT<Dual<3>>(S, dvec<3>(d, 0), dconst<3>(b.aux4[j].z), mk, -pj4.w), 0);
+            gx += (rk.w * (-pj4.w / b.vel4[j].w)) * gW;
+            // k in num / den of sand j: (e_f,k n + m) V_k W(x_j - x_k), V_k = m_k / rho_k
             const float4 rj = A.r[j];
-            const auto w = poly6T<Dual<5>>(S, lenT(dvec<5>(-1.f * d, 0)));
-            const auto vj = mk / dseed<5>(rhoK, 4);
-            const auto t = rj.x * (dseed<5>(epsfK, 3) * vj * w) + rj.y * (vj * w);
-            gx += -grad3(t, 0);
-            geps += t.d[3];
-            grho += t.d[4];
-        });
+            const float Vk = mk / rhoK;
+            const float W = poly6(S, len3(d));
+            const float s = rj.x * epsfK + rj.y;
+            gx += (s * Vk) * gW;
+            geps += rj.x * Vk * W;
+            grho += s * (-mk / (rhoK * rhoK)) * W;
+        }
+        float4 s = A.s[slot];
+        s.x += grho;
+        s.z += geps;
+        A.s[slot] = s;
     }
     add3(A.x[slot], gx);
-    float4 s = A.s[slot];
-    s.x += grho;
-    s.z += geps;
-    s.w += gsat;
-    A.s[slot] = s;
 }
 
 // A5a: sand: average flow = num / sat, sat = sum V_j W -> (num-bar, sat-bar total).
@@ -610,41 +775,43 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjFlowPairs(const SceneDev* __re
     if (pk4.w == 0.f) return;
     const float3 xk = xyz(pk4);
     float3 gx = mk3(0.f, 0.f, 0.f), gv = gx;
-    float grho = 0.f;
     if (pk4.w < 0.f) {
         const float4 rk = A.r[slot];
         const float vk = -pk4.w / b.vel4[slot].w;
-        forWaterNeighbors(S, b.lists, slot, xk, b.pos4, [&](int j) {
+        LabelCursor<false> wc(S, b.lists, slot, xk, b.pos4);
+        for (int j; wc.next(j);) {
             const float4 pj4 = b.pos4[j];
             const float4 vj4 = b.vel4[j];
-            // own sums: v_j V_j W and V_j W, d = x_k - x_j
+            const float3 gW = poly6Grad(S, xk - xyz(pj4));  // d W(x_k - x_j) / d x_k = d W(x_j - x_k) / d x_k
+            // own sums v_j V_j W and V_j W; k in the fluid voidage 1 - V_k W of water j
             const float vj = pj4.w / vj4.w;
-            gx += (vj * (dot3(xyz(rk), xyz(vj4)) + rk.w)) * poly6Grad(S, xk - xyz(pj4));
-            // k in the fluid voidage of water j: -V_k W(x_j - x_k)
-            gx += (A.s[j].z * vk) * poly6Grad(S, xyz(pj4) - xk);
-        });
+            gx += (vj * (dot3(xyz(rk), xyz(vj4)) + rk.w) - A.s[j].z * vk) * gW;
+        }
     } else {
         const float mk = pk4.w;
         const float ek = A.s[slot].z;
         const float3 vk3 = xyz(b.vel4[slot]);
         const float rhoK = b.vel4[slot].w;
-        forSandNeighbors(S, b.lists, slot, xk, b.pos4, [&](int j) {
+        const float Vk = mk / rhoK;
+        float grho = 0.f;
+        LabelCursor<true> sc(S, b.lists, slot, xk, b.pos4);
+        for (int j; sc.next(j);) {
             const float4 pj4 = b.pos4[j];
             const float3 d = xk - xyz(pj4);
-            // own fluid voidage 1 - sum V_j W(x_k - x_j)
-            gx += (-ek * (-pj4.w / b.vel4[j].w)) * poly6Grad(S, d);
-            // k in the flow / saturation sums of sand j: d = x_j - x_k; seeds d 0-2, rho_k 3
+            const float3 gW = poly6Grad(S, d);
+            // own fluid voidage 1 - sum V_j W(x_k - x_j), and k in the flow /
+            // saturation sums of sand j: V_k W(x_j - x_k) (v_k, 1)
             const float4 rj = A.r[j];
-            const auto t = (mk / dseed<4>(rhoK, 3)) * poly6T<Dual<4>>(S, lenT(dvec<4>(-1.f * d, 0)));
             const float s = dot3(xyz(rj), vk3) + rj.w;
-            gx += -s * grad3(t, 0);
-            grho += s * t.d[3];
-            gv += t.v * xyz(rj);
-        });
+            gx += (ek * pj4.w / b.vel4[j].w + s * Vk) * gW;
+            const float W = poly6(S, len3(d));
+            grho += s * (-mk / (rhoK * rhoK)) * W;
+            gv += (Vk * W) * xyz(rj);
+        }
+        A.s[slot].x += grho;
     }
     add3(A.x[slot], gx);
     add3(A.v[slot], gv);
-    A.s[slot].x += grho;
 }
 
 // A6a: water: density cotangent including the pressure path.
@@ -678,15 +845,17 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjDensityPairs(const SceneDev* _
     const float mk = pk4.w;
     const float rk = A.r[slot].x;
     float3 gx = mk3(0.f, 0.f, 0.f);
-    forWaterNeighbors(S, b.lists, slot, xk, b.pos4, [&](int j) {
-        if (j == slot) return;
+    LabelCursor<false> wc(S, b.lists, slot, xk, b.pos4);
+    for (int j; wc.next(j);) {
+        if (j == slot) continue;
         const float4 pj4 = b.pos4[j];
         gx += (rk * pj4.w + A.r[j].x * mk) * poly6Grad(S, xk - xyz(pj4));
-    });
-    forBoundaryNeighbors(S, b.lists, slot, xk, b.bpos4, [&](int bb) {
+    }
+    BoundaryCursor bc(S, b.lists, slot, xk, b.bpos4);
+    for (int bb; bc.next(bb);) {
         const float4 bj = b.bpos4[bb];
         gx += (rk * S.rho0 * fabsf(bj.w)) * poly6Grad(S, xk - xyz(bj));
-    });
+    }
     add3(A.x[slot], gx);
 }
 
