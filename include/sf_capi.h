@@ -261,10 +261,13 @@ const char* sf_last_error_string(const sf_handle* h);
  * Runs n_substeps substeps of every scene at the fixed dt from the current
  * state (the same trajectory sf_substeps_fixed computes), evaluates per scene
  *     L = (1 / N_sand) * sum over sand particles of |x_T - target|^2
- * and back-propagates it through every substep. State is checkpointed every
- * checkpoint_every substeps and recomputed segment by segment, so device
- * memory grows with n_substeps / checkpoint_every + checkpoint_every states
- * (76 bytes per slot each).
+ * and back-propagates it through every substep. The substeps of one segment
+ * of checkpoint_every substeps are stored as they run (neighbour lists and
+ * intermediate fields, about 0.7 KB per particle slot and substep); earlier
+ * segments keep only a checkpoint of their starting state (76 bytes per slot)
+ * and are recomputed once in the reverse sweep. checkpoint_every >= n_substeps
+ * stores the whole trajectory and recomputes nothing (fastest); smaller values
+ * trade one extra forward pass for memory.
  *
  * Arrays are scene-major over the handle's scenes and ordered by particle id
  * within a scene (the creation order), 3 floats per particle:

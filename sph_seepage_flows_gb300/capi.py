@@ -248,13 +248,16 @@ class Simulation:
         return out
 
     # -------------------------------------------------------------- adjoint
-    def adjoint(self, dt: float, n_substeps: int, target, checkpoint_every: int = 1,
+    def adjoint(self, dt: float, n_substeps: int, target, checkpoint_every: int | None = None,
                 want_state_grads: bool = True) -> dict:
         """Runs n_substeps at the fixed dt and back-propagates the per-scene loss
         mean_sand |x_T - target|^2 (sf_adjoint_run). target: (sum n, 3), scene-major,
-        id order. Returns loss (n_scenes,), grad_params (n_scenes, 3: tan friction
-        angle, capillary scale, permeability scale), grad_pos0 / grad_vel0
-        (sum n, 3, id order) and the forward / reverse device milliseconds."""
+        id order. checkpoint_every: substeps stored per segment (default: all,
+        no recomputation). Returns loss (n_scenes,), grad_params (n_scenes, 3: tan
+        friction angle, capillary scale, permeability scale), grad_pos0 /
+        grad_vel0 (sum n, 3, id order) and the forward / reverse device milliseconds."""
+        if checkpoint_every is None:
+            checkpoint_every = n_substeps
         ns = len(self.scenes)
         total = sum(self.size(s) for s in range(ns))
         tgt = np.ascontiguousarray(target, dtype=np.float32).reshape(-1)

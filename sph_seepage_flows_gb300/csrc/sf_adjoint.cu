@@ -869,7 +869,22 @@ __global__ void kAdjFinish(const SceneDev* __restrict__ scenes, const int* __res
     A.adjV[id] = A.v[slot];
 }
 
+__global__ void kAdjStore(PassBuffers b, const int* __restrict__ pid, AdjSlab s) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    s.pos[slot] = b.pos4[slot];
+    s.vel[slot] = b.vel4[slot];
+    s.acc[slot] = b.acc4[slot];
+    s.adh[slot] = b.adh4[slot];
+    s.avgadh[slot] = b.avgadh4[slot];
+    s.mat[slot] = b.mat4[slot];
+    s.pid[slot] = pid[slot];
+}
+
 // ------------------------------------------------------------ launchers
+void launchAdjStore(const LaunchCtx& c, const PassBuffers& b, const int* pid, const AdjSlab& s) {
+    kAdjStore<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(b, pid, s);
+}
+
 void launchAdjSeed(const LaunchCtx& c, const float4* pos4, const int* pid, const float* target, float4* adjX,
                    float4* adjV, float2* lossPartial) {
     kAdjSeed<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, pos4, pid, target, adjX, adjV,

@@ -23,6 +23,24 @@ struct AdjBuffers {
     float4* s;       // (density, pressure, voidage, saturation) cotangents
 };
 
+// Everything the adjoint of one substep reads, stored by its forward pass:
+// the neighbour lists, the cell table and the per-slot fields in sorted
+// order as they stand after the water-momentum pass (before integration).
+struct AdjSlab {
+    unsigned int* cnt;
+    unsigned int* nbr;
+    int* bcnt;
+    unsigned int* bnbr;
+    int* ccnt;
+    unsigned int* cnbr;
+    unsigned int* cs;
+    float4 *aux, *flow, *drag, *acc, *adh, *avgadh, *pos, *vel, *mat;
+    int* pid;
+};
+// Copies the fields the integrator overwrites (pos, vel, acc, adhesion,
+// average adhesion) and the sorted mat / pid into the slab.
+void launchAdjStore(const LaunchCtx& c, const PassBuffers& b, const int* pid, const AdjSlab& s);
+
 // Seeds adjX / adjV from L = mean over sand of |x - target|^2 (target indexed
 // like adjX), written unnormalised (2 (x - target)); lossPartial[block] =
 // (sum of |x - target|^2 over the block's sand, sand count).

@@ -214,6 +214,8 @@ struct sf_handle {
     float2* adjLoss = nullptr;    // 1 per slot block
     char* snap = nullptr;         // state snapshots for checkpointing
     size_t snapBytes = 0;
+    char* slab = nullptr;         // stored substeps of one checkpoint segment
+    size_t slabBytes = 0;
     std::string err;
 
     sf_status fail(sf_status st, const std::string& msg) {
@@ -312,6 +314,7 @@ struct sf_handle {
         devFree(adjParam);
         devFree(adjLoss);
         devFree(snap);
+        devFree(slab);
         if (stage) cudaFree(stage);
         if (ownStream && stream) cudaStreamDestroy(stream);
     }
@@ -1072,7 +1075,117 @@ sf_status snapCopy(sf_handle* h, char* snap, bool save) {
     return SF_OK;
 }
 
-sf_status ensureAdjoint(sf_handle* h, size_t snapshots) {
+// One slab = what the adjoint of one substep reads (AdjSlab), 256-byte aligned.
+size_t slabStride(const sf_handle* h) {
+    const size_t M = size_t(h->totalSlots);
+    const size_t b = M * (sizeof(unsigned) * (1 + kMaxNbr + kMaxContact) + sizeof(int) * 2 + sizeof(unsigned) * kMaxBNbr +
+                          9 * sizeof(float4) + sizeof(int)) +
+                     sizeof(unsigned) * (size_t(h->totalCells) + 1);
+    return (b + 255) / 256 * 256;
+}
+
+AdjSlab slabAt(const sf_handle* h, char* base) {
+    const size_t M = size_t(h->totalSlots);
+    AdjSlab s;
+    char* p = base;
+    auto take = [&](size_t bytes) {
+        char* r = p;
+        p += bytes;
+        return r;
+    };
+    s.pos = reinterpret_cast<float4*>(take(sizeof(float4) * M));
+    s.vel = reinterpret_cast<float4*>(take(sizeof(float4) * M));
+    s.aux = reinterpret_cast<float4*>(take(sizeof(float4) * M));
+    s.flow = reinterpret_cast<float4*>(take(sizeof(float4) * M));
+    s.drag = reinterpret_cast<float4*>(take(sizeof(float4) * M));
+    s.acc = reinterpret_cast<float4*>(take(sizeof(float4) * M));
+    s.adh = reinterpret_cast<float4*>(take(sizeof(float4) * M));
+    s.avgadh = reinterpret_cast<float4*>(take(sizeof(float4) * M));
+    s.mat = reinterpret_cast<float4*>(take(sizeof(float4) * M));
+    s.nbr = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * M * kMaxNbr));
+    s.bnbr = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * M * kMaxBNbr));
+    s.cnbr = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * M * kMaxContact));
+    s.cnt = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * M));
+    s.bcnt = reinterpret_cast<int*>(take(sizeof(int) * M));
+    s.ccnt = reinterpret_cast<int*>(take(sizeof(int) * M));
+    s.pid = reinterpret_cast<int*>(take(sizeof(int) * M));
+    s.cs = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * (size_t(h->totalCells) + 1)));
+    return s;
+}
+
+// The pass buffers of a stored substep.
+PassBuffers slabBuffers(const sf_handle* h, const AdjSlab& s) {
+    PassBuffers b = h->buffers();
+    b.lists.cnt = s.cnt;
+    b.lists.nbr = s.nbr;
+    b.lists.bcnt = s.bcnt;
+    b.lists.bnbr = s.bnbr;
+    b.lists.ccnt = s.ccnt;
+    b.lists.cnbr = s.cnbr;
+    b.lists.cs = s.cs;
+    b.listsW = NbrListsW{s.cnt, s.nbr, s.bcnt, s.bnbr, s.ccnt, s.cnbr, s.cs, h->bcs, b.lists.M};
+    b.pos4 = s.pos;
+    b.vel4 = s.vel;
+    b.aux4 = s.aux;
+    b.flow4 = s.flow;
+    b.drag4 = s.drag;
+    b.acc4 = s.acc;
+    b.adh4 = s.adh;
+    b.avgadh4 = s.avgadh;
+    b.mat4 = s.mat;
+    b.col4 = nullptr;
+    return b;
+}
+
+// One fixed-dt substep whose lists, cell table and per-substep fields are
+// written straight into the slab (the handle's own buffers are swapped out
+// for the passes that produce them), with the fields the integrator
+// overwrites copied in before it runs.
+sf_status runSubstepStore(sf_handle* h, float dt, const AdjSlab& s) {
+    unsigned *cnt = h->nbrCnt, *nbr = h->nbr, *bnbr = h->bnbr, *cnbr = h->cnbr, *cs = h->cs;
+    int *bcnt = h->bnbrCnt, *ccnt = h->cnbrCnt;
+    float4 *aux = h->aux, *flow = h->flow, *drag = h->drag;
+    h->nbrCnt = s.cnt;
+    h->nbr = s.nbr;
+    h->bnbr = s.bnbr;
+    h->cnbr = s.cnbr;
+    h->cs = s.cs;
+    h->bnbrCnt = s.bcnt;
+    h->cnbrCnt = s.ccnt;
+    h->aux = s.aux;
+    h->flow = s.flow;
+    h->drag = s.drag;
+    sf_status st = SF_OK;
+    for (int k = SF_STAGE_SORT; k <= SF_STAGE_WATER_MOMENTUM && st == SF_OK; ++k) st = runStage(h, k, dt, 0);
+    if (st == SF_OK) {
+        launchAdjStore(h->ctx(), h->buffers(), h->pid[h->cur], s);
+        h->launches += 1;
+    }
+    h->nbrCnt = cnt;
+    h->nbr = nbr;
+    h->bnbr = bnbr;
+    h->cnbr = cnbr;
+    h->cs = cs;
+    h->bnbrCnt = bcnt;
+    h->cnbrCnt = ccnt;
+    h->aux = aux;
+    h->flow = flow;
+    h->drag = drag;
+    if (st != SF_OK) return st;
+    return runStage(h, SF_STAGE_INTEGRATE, dt, 0);
+}
+
+sf_status growBuffer(sf_handle* h, char*& p, size_t& have, size_t need, const char* what) {
+    if (have >= need) return SF_OK;
+    if (p && h->cuda(cudaStreamSynchronize(h->stream), "sync before realloc")) return SF_ERR_CUDA;
+    devFree(p);
+    have = 0;
+    if (h->cuda(cudaMalloc(reinterpret_cast<void**>(&p), need), what)) return SF_ERR_CUDA;
+    have = need;
+    return SF_OK;
+}
+
+sf_status ensureAdjoint(sf_handle* h, size_t snapshots, size_t slabs) {
     const size_t M = size_t(h->totalSlots);
     if (!h->adj.adjX) {
         for (float4** p : {&h->adj.adjX, &h->adj.adjV, &h->adj.x, &h->adj.v, &h->adj.acc, &h->adj.flow, &h->adj.adh,
@@ -1089,14 +1202,10 @@ sf_status ensureAdjoint(sf_handle* h, size_t snapshots) {
             h->cuda(cudaMemsetAsync(h->adjTarget, 0, sizeof(float) * 3 * M, h->stream), "cudaMemset target"))
             return SF_ERR_CUDA;
     }
-    const size_t need = snapshots * snapStride(h);
-    if (h->snapBytes < need) {
-        if (h->snap && h->cuda(cudaStreamSynchronize(h->stream), "sync before snapshot realloc")) return SF_ERR_CUDA;
-        devFree(h->snap);
-        h->snapBytes = 0;
-        if (h->cuda(cudaMalloc(reinterpret_cast<void**>(&h->snap), need), "cudaMalloc snapshots")) return SF_ERR_CUDA;
-        h->snapBytes = need;
-    }
+    if (growBuffer(h, h->snap, h->snapBytes, snapshots * snapStride(h), "cudaMalloc snapshots")) return SF_ERR_CUDA;
+    if (growBuffer(h, h->slab, h->slabBytes, slabs * slabStride(h),
+                   "cudaMalloc stored substeps (lower checkpoint_every to use less memory)"))
+        return SF_ERR_CUDA;
     return SF_OK;
 }
 
@@ -1112,12 +1221,13 @@ sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t che
     if (checkpoint_every < 1) return h->fail(SF_ERR_INVALID, "checkpoint_every must be >= 1");
     const int64_t T = n_substeps, K = std::min(checkpoint_every, n_substeps);
     const int64_t nSeg = (T + K - 1) / K;
-    // snapshot slots: [0, nSeg) checkpoints, then states 1 .. K-1 of a segment, then the final state
-    const int64_t nSnap = nSeg + (K - 1) + 1;
-    if (ensureAdjoint(h, size_t(nSnap))) return SF_ERR_CUDA;
-    const size_t stride = snapStride(h);
-    auto snapAt = [&](int64_t k) { return h->snap + size_t(k) * stride; };
-    char* finalSnap = snapAt(nSnap - 1);
+    const int64_t lastLen = T - (nSeg - 1) * K;
+    // snapshots: segment starts [0, nSeg - 1) and the final state; slabs: one segment
+    if (ensureAdjoint(h, size_t(nSeg), size_t(K))) return SF_ERR_CUDA;
+    const size_t sStride = snapStride(h), lStride = slabStride(h);
+    auto snapAt = [&](int64_t k) { return h->snap + size_t(k) * sStride; };
+    auto slab = [&](int64_t t) { return slabAt(h, h->slab + size_t(t) * lStride); };
+    char* finalSnap = snapAt(nSeg - 1);
 
     // targets into the slot_off + id layout
     int64_t off = 0;
@@ -1141,14 +1251,16 @@ sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t che
     } guard{ev};
     cudaEventRecord(ev[0], h->stream);
 
-    // forward pass with a checkpoint at the start of every segment
+    // forward: a checkpoint at the start of every segment but the last, whose
+    // substeps are stored as they run
     sf_status st = SF_OK;
-    for (int64_t seg = 0; seg < nSeg; ++seg) {
+    for (int64_t seg = 0; seg + 1 < nSeg; ++seg) {
         if ((st = snapCopy(h, snapAt(seg), true))) return st;
-        if ((st = sf_substeps_fixed(h, dt, std::min(K, T - seg * K)))) return st;
+        if ((st = sf_substeps_fixed(h, dt, K))) return st;
     }
-    LaunchCtx c = h->ctx();
-    launchAdjSeed(c, h->pos[h->cur], h->pid[h->cur], h->adjTarget, h->adj.adjX, h->adj.adjV, h->adjLoss);
+    for (int64_t t = 0; t < lastLen; ++t)
+        if ((st = runSubstepStore(h, dt, slab(t)))) return st;
+    launchAdjSeed(h->ctx(), h->pos[h->cur], h->pid[h->cur], h->adjTarget, h->adj.adjX, h->adj.adjV, h->adjLoss);
     h->launches += 1;
     if ((st = snapCopy(h, finalSnap, true))) return st;
     if (h->cuda(cudaMemsetAsync(h->adjParam, 0, sizeof(float) * 3 * size_t(h->slotBlocks), h->stream),
@@ -1156,21 +1268,18 @@ sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t che
         return SF_ERR_CUDA;
     cudaEventRecord(ev[1], h->stream);
 
-    // reverse pass, segment by segment
+    // reverse, segment by segment: recompute and store a segment, then run
+    // its substeps' adjoints backwards
     for (int64_t seg = nSeg - 1; seg >= 0; --seg) {
-        const int64_t len = std::min(K, T - seg * K);
-        if (len > 1) {  // states of the segment's substeps 1 .. len-1
+        const int64_t len = seg == nSeg - 1 ? lastLen : K;
+        if (seg != nSeg - 1) {
             if ((st = snapCopy(h, snapAt(seg), false))) return st;
-            for (int64_t t = 1; t < len; ++t) {
-                if ((st = runSubstep(h, dt, 0))) return st;
-                if ((st = snapCopy(h, snapAt(nSeg + t - 1), true))) return st;
-            }
+            for (int64_t t = 0; t < len; ++t)
+                if ((st = runSubstepStore(h, dt, slab(t)))) return st;
         }
         for (int64_t t = len - 1; t >= 0; --t) {
-            if ((st = snapCopy(h, t == 0 ? snapAt(seg) : snapAt(nSeg + t - 1), false))) return st;
-            for (int s = SF_STAGE_SORT; s <= SF_STAGE_WATER_MOMENTUM; ++s)
-                if ((st = runStage(h, s, dt, 0))) return st;
-            h->launches += launchAdjSubstep(h->ctx(), h->adj, h->buffers(), h->pid[h->cur], dt, h->adjParam);
+            const AdjSlab sl = slab(t);
+            h->launches += launchAdjSubstep(h->ctx(), h->adj, slabBuffers(h, sl), sl.pid, dt, h->adjParam);
             if (h->cuda(cudaGetLastError(), "adjoint launch")) return SF_ERR_CUDA;
         }
     }
