@@ -20,6 +20,11 @@ reference has no CPU physics, so this is the FP32 CPU restatement of its
 kernels (oracle/, pinned bit-exact to the reference kernels), on all host
 threads, one substep of the same scene per step.
 
+Also reported (same GPU, device time): "batched", the 64-scene ensemble in
+one handle against a loop of per-scene handles; "adjoint", the 20k-particle
+column over 200 substeps, gradient run (sf_adjoint_run) against a forward run;
+"calibration", per-iteration time of the 32-scene batched Adam calibration.
+
 Multi-GPU: scenes are independent replicas (no collective); under torchrun
 every rank runs its own copy and value = sum over ranks (weak scaling).
 """
@@ -190,6 +195,67 @@ def batched_comparison(stream, substeps=100, n_scenes=64, blocks=2):
             "unit": "particle-substeps/s", "device_error_flags": flags}
 
 
+def adjoint_comparison(stream, n_substeps=200, checkpoint_every=20):
+    """The adjoint workload: the 20k-particle sand column collapsing for
+    n_substeps at the reference dt; loss = mean squared distance of the final
+    sand positions to a forward run with tan friction angle, capillary and
+    permeability scales +10%. Gradient run (sf_adjoint_run: forward with
+    checkpoints + reverse sweep) against a plain forward run of the same
+    substeps, both device-timed."""
+    import torch
+
+    from sph_seepage_flows_gb300 import calibrate, capi, scenes
+    sc = scenes.adjoint_column()
+    dt = reference_dt(sc)
+    theta0 = np.array([sc.params.dem_tan_friction_angle, 1.0, 1.0])
+    target = calibrate.forward_targets([sc], [theta0 * 1.1], dt, n_substeps)[0]
+    fwd = capi.Simulation(sc, stream=stream.cuda_stream)
+    tuning = fwd.autotune(dt)
+    fwd.substeps_fixed(dt, 2)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fwd.substeps_fixed(dt, n_substeps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_fwd = e0.elapsed_time(e1)
+    fwd.close()
+    out = {"workload": "adjoint_column", "particles": sc.n, "substeps": n_substeps, "dt": dt,
+           "forward_ms": ms_fwd, "tuning": tuning, "runs": {}}
+    for k in (checkpoint_every, n_substeps):
+        sim = capi.Simulation(sc, stream=stream.cuda_stream)
+        sim.autotune(dt)
+        sim.adjoint(dt, n_substeps, target, checkpoint_every=k, want_state_grads=False)  # allocates
+        calibrate.reset_state(sim, 0, sc)
+        r = sim.adjoint(dt, n_substeps, target, checkpoint_every=k)
+        sim.close()
+        out["runs"][str(k)] = {
+            "checkpoint_every": k, "forward_ms": r["ms_forward"], "reverse_ms": r["ms_reverse"],
+            "gradient_run_vs_forward": (r["ms_forward"] + r["ms_reverse"]) / ms_fwd,
+            "reverse_vs_forward": r["ms_reverse"] / ms_fwd,
+            "loss": float(r["loss"][0]), "grad_params": [float(v) for v in r["grad_params"][0]],
+            "grad_vel0_norm": float(np.linalg.norm(r["grad_vel0"]))}
+    return out
+
+
+def calibration_timing(stream, iterations=2, n_substeps=500, checkpoint_every=25):
+    """Per-iteration time of the batched calibration workload (32 scenes of
+    10k-50k particles, 500 substeps, checkpoints every 25): `iterations`
+    Adam iterations of one batched adjoint launch each."""
+    from sph_seepage_flows_gb300 import calibrate
+    scs, theta0, theta_true, dt = calibrate.workload()
+    targets = calibrate.forward_targets(scs, theta_true, dt, n_substeps)
+    h = calibrate.calibrate(scs, targets, theta0, dt, n_substeps, checkpoint_every, iterations)
+    ms = h["ms"]
+    return {"scenes": len(scs), "particles": int(sum(s.n for s in scs)), "substeps": n_substeps,
+            "checkpoint_every": checkpoint_every, "iterations_timed": iterations,
+            "device_ms_per_iteration": float(np.median([m["forward"] + m["reverse"] for m in ms])),
+            "wall_ms_per_iteration": float(np.median([m["wall"] for m in ms])),
+            "particle_substeps_per_s_forward_and_reverse":
+                float(sum(s.n for s in scs) * n_substeps / (np.median([m["forward"] + m["reverse"] for m in ms]) * 1e-3)),
+            "loss_mean_by_iteration": [float(np.mean(l)) for l in h["loss"]]}
+
+
 def run_reference(args, rank, world):
     """--impl reference: the reference kernels' FP32 CPU restatement."""
     if rank != 0:
@@ -238,6 +304,7 @@ def run_ours(args, rank, world):
         if world > 1:
             torch.distributed.barrier()
 
+    tuning = sim.autotune(dt)  # list capacity and per-pass block sizes for this scene
     # warm-up (also captures the two-substep graph)
     sim.substeps_fixed(dt, 2 * max(1, (args.warmup + 1) // 2))
     sim.synchronize()
@@ -321,6 +388,8 @@ def run_ours(args, rank, world):
     lab = sim.field("label")
     pairs = int(4 * nbrs[lab == 0].sum() + 3 * nbrs[lab == 1].sum())
     batched = None if args.no_batched else batched_comparison(stream)
+    adjoint = None if args.no_adjoint else adjoint_comparison(stream)
+    calib = None if args.no_calibration else calibration_timing(stream)
     if rank != 0:
         return
     cpu = None if args.no_cpu else cpu_baseline(sc, dt)
@@ -332,7 +401,7 @@ def run_ours(args, rank, world):
         "config": {"workload": args.workload, "particles": n, "sand": sc.n_sand, "water": sc.n_water,
                    "boundary": sc.nb, "grid": list(sc.bparams.grid_size), "dt": dt,
                    "l2": "working set ~250 B/particle > L2 (no flush needed)" if n >= 600_000 else "flushed",
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}", "tuning": tuning},
         "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": NCU_TRAFFIC.get(top) if args.workload == "plain_large" else None,
@@ -349,6 +418,8 @@ def run_ours(args, rank, world):
         "e2e": e2e,
         "cpu_baseline": cpu,
         "batched": batched,
+        "adjoint": adjoint,
+        "calibration": calib,
     }
     print(json.dumps(line), flush=True)
 
@@ -363,6 +434,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-calibration", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -25,6 +25,7 @@
  *   sf_substeps_fixed    fixed-substep mode of main.cpp:250-258 (no reference counterpart for the graph capture)
  *   sf_create_batched    no reference counterpart (independent scenes in one launch)
  *   sf_adjoint_run       no reference counterpart (reverse-mode gradient of a trajectory loss)
+ *   sf_autotune          no reference counterpart (list capacity and block sizes of the passes)
  *
  * Threading: handles are independent; one handle must not be used from two
  * host threads at once. All work is issued on the stream given at creation.
@@ -248,9 +249,20 @@ sf_status sf_synchronize(sf_handle* h);
  * every kernel node). */
 sf_status sf_launch_count(const sf_handle* h, int64_t* launches);
 
-/* Launch configuration of the neighbor passes: block size (multiple of 32,
- * <= 1024) and the number of particles each thread handles; 0 keeps a value. */
+/* Launch configuration of the passes: threads per block (32, 64, 128 or 256)
+ * for every tuned pass, and the particles each thread handles (1); 0 keeps a
+ * value. Takes effect at the next substep (captured graphs are dropped). */
 sf_status sf_set_tuning(sf_handle* h, int32_t block_size, int32_t items_per_thread);
+
+/* Autotuner (no reference counterpart). Sizes the neighbour lists for the
+ * current state (list capacity = largest neighbour count + 25%, a multiple of
+ * 32 in [64, 256]; sf_create does this once for the initial state) and picks
+ * the fastest block size (64, 128 or 256 threads) for each neighbour pass by
+ * timing it on the current state with CUDA events (density, average flow,
+ * voidage/adhesion, sand momentum, water momentum; the integrator keeps its
+ * size). The state is not advanced. block_sizes_out (6 entries, in that pass
+ * order then the integrator) and list_capacity_out may be NULL. */
+sf_status sf_autotune(sf_handle* h, float dt, int32_t* block_sizes_out, int32_t* list_capacity_out);
 
 /* Text of the last error on this handle (or of the last failed create when h is NULL). */
 const char* sf_last_error_string(const sf_handle* h);

@@ -80,6 +80,7 @@ def load(path: str = LIB_PATH):
         "sf_synchronize": (i32, [H]),
         "sf_launch_count": (i32, [H, P(i64)]),
         "sf_set_tuning": (i32, [H, i32, i32]),
+        "sf_autotune": (i32, [H, f32, P(i32), P(i32)]),
         "sf_last_error_string": (ctypes.c_char_p, [H]),
         "sf_adjoint_run": (i32, [H, f32, i64, i64, P(f32), P(f32), P(f32), P(f32), P(f32), P(f32)]),
         "sf_cell_sort_noalloc": (i32, [P(SfBoundaryParams), ctypes.c_void_p, i64, ctypes.c_void_p, ctypes.c_void_p,
@@ -246,6 +247,17 @@ class Simulation:
         self._check(self.lib.sf_get_cell_table(self.h, scene, which,
                                                out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), out.size))
         return out
+
+    def set_tuning(self, block_size: int, items_per_thread: int = 0):
+        self._check(self.lib.sf_set_tuning(self.h, int(block_size), int(items_per_thread)))
+
+    def autotune(self, dt: float) -> dict:
+        """sf_autotune: list capacity and per-pass block sizes for the current state."""
+        bs = (ctypes.c_int32 * 6)()
+        cap = ctypes.c_int32()
+        self._check(self.lib.sf_autotune(self.h, float(dt), bs, ctypes.byref(cap)))
+        names = ["density", "avgflow", "voidage_adhesion", "sand_momentum", "water_momentum", "integrate"]
+        return {"block_sizes": dict(zip(names, list(bs))), "list_capacity": cap.value}
 
     # -------------------------------------------------------------- adjoint
     def adjoint(self, dt: float, n_substeps: int, target, checkpoint_every: int | None = None,

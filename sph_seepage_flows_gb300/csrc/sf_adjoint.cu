@@ -64,9 +64,9 @@ template <bool kSand> struct LabelCursor {
                                            const float4* __restrict__ pos)
         : S(&s), cs(L.cs), pos4(pos), pi(p_i), k(0), j(0), jEnd(0) {
         const unsigned c = L.cnt[slot];
-        stencil = int(c & 0xFFFFu) + int(c >> 16) > kMaxNbr;
+        stencil = int(c & 0xFFFFu) + int(c >> 16) > L.cap;
         n = kSand ? int(c & 0xFFFFu) : int(c >> 16);
-        p = L.nbr + slot + (kSand ? size_t(0) : size_t(kMaxNbr - 1) * size_t(L.M));
+        p = L.nbr + slot + (kSand ? size_t(0) : size_t(L.cap - 1) * size_t(L.M));
         step = kSand ? L.M : -L.M;
         x = x1 = y = y0 = y1 = z0 = z1 = 0;
         if (stencil) {

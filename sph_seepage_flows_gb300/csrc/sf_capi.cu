@@ -207,6 +207,9 @@ struct sf_handle {
     bool sorted = false;
     int64_t launches = 0;
     GraphCache graph[2];
+    int nbrCap = kMinNbr;                 // particle neighbour list capacity (per slot)
+    int block[kTunedPasses] = {kSlotAlign, kSlotAlign, kSlotAlign, kSlotAlign, kSlotAlign, kSlotAlign};
+    unsigned int* dProbe = nullptr;       // neighbour-count probe word
     // reverse-mode buffers, allocated by the first sf_adjoint_run
     AdjBuffers adj{};
     float* adjTarget = nullptr;   // 3 floats per slot, indexed by slot_off + id
@@ -235,6 +238,7 @@ struct sf_handle {
         c.state = dState;
         c.errWord = dErr;
         c.slotBlocks = slotBlocks;
+        for (int k = 0; k < kTunedPasses; ++k) c.block[k] = block[k];
         return c;
     }
     PassBuffers buffers() const {
@@ -248,6 +252,7 @@ struct sf_handle {
         b.listsW.cs = cs;
         b.listsW.bcs = bcs;
         b.listsW.M = totalSlots;
+        b.listsW.cap = nbrCap;
         b.lists.cnt = nbrCnt;
         b.lists.nbr = nbr;
         b.lists.bcnt = bnbrCnt;
@@ -257,6 +262,7 @@ struct sf_handle {
         b.lists.cs = cs;
         b.lists.bcs = bcs;
         b.lists.M = totalSlots;
+        b.lists.cap = nbrCap;
         b.pos4 = pos[cur];
         b.vel4 = vel[cur];
         b.aux4 = aux;
@@ -270,9 +276,19 @@ struct sf_handle {
         b.bpos4 = bpos;
         return b;
     }
+    // Drop the captured substep graphs (after a change of buffers or launch shapes).
+    void dropGraphs() {
+        for (auto& g : graph) {
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+            g.dt = 0.f;
+            g.nodes = 0;
+        }
+    }
     ~sf_handle() {
         for (auto& g : graph)
             if (g.exec) cudaGraphExecDestroy(g.exec);
+        devFree(dProbe);
         for (int k = 0; k < 2; ++k) {
             devFree(pos[k]);
             devFree(vel[k]);
@@ -360,6 +376,54 @@ sf_status runSubstep(sf_handle* h, float timeArg, int adaptive) {
         sf_status st = runStage(h, s, timeArg, adaptive);
         if (st != SF_OK) return st;
     }
+    return SF_OK;
+}
+
+// List capacity for a largest neighbour count: 25% + 8 headroom, a multiple
+// of 32 in [kMinNbr, kMaxNbr].
+int capacityFor(unsigned maxCount) {
+    const int want = int(maxCount + maxCount / 4u + 8u);
+    return std::min(kMaxNbr, std::max(kMinNbr, (want + 31) / 32 * 32));
+}
+
+// Largest neighbour count of the current state: a sort into the other buffer
+// set, the count kernel, then the buffer set and the "not sorted" flag are
+// put back (the state itself is unchanged).
+sf_status countNeighborsMax(sf_handle* h, unsigned* maxCount) {
+    const int cur = h->cur;
+    const bool sorted = h->sorted;
+    sf_status st = runSort(h);
+    if (st) return st;
+    if (h->cuda(cudaMemsetAsync(h->dProbe, 0, sizeof(unsigned), h->stream), "probe clear")) return SF_ERR_CUDA;
+    launchNeighborCountMax(h->ctx(), h->pos[h->cur], h->cs, h->dProbe);
+    h->launches += 1;
+    if (h->cuda(cudaMemcpyAsync(maxCount, h->dProbe, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream),
+                "probe read") ||
+        h->cuda(cudaStreamSynchronize(h->stream), "probe sync"))
+        return SF_ERR_CUDA;
+    if (!sorted) {
+        h->cur = cur;
+        h->sorted = false;
+    }
+    return SF_OK;
+}
+
+// (Re)allocates the particle lists for the capacity the current state needs.
+sf_status probeListCapacity(sf_handle* h) {
+    unsigned mx = 0;
+    sf_status st = countNeighborsMax(h, &mx);
+    if (st) return st;
+    const int cap = capacityFor(mx);
+    if (h->nbr && cap == h->nbrCap) return SF_OK;
+    if (h->nbr && h->cuda(cudaStreamSynchronize(h->stream), "sync before list realloc")) return SF_ERR_CUDA;
+    devFree(h->nbr);
+    if (h->cuda(cudaMalloc(reinterpret_cast<void**>(&h->nbr), sizeof(unsigned) * size_t(h->totalSlots) * cap),
+                "cudaMalloc neighbour lists") ||
+        h->cuda(cudaMemsetAsync(h->nbr, 0, sizeof(unsigned) * size_t(h->totalSlots) * cap, h->stream),
+                "cudaMemset neighbour lists"))
+        return SF_ERR_CUDA;
+    h->nbrCap = cap;
+    h->dropGraphs();
     return SF_OK;
 }
 
@@ -499,7 +563,6 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
     SF_ALLOC(h->keys, sizeof(unsigned) * M);
     SF_ALLOC(h->nbrCnt, sizeof(unsigned) * M);
     SF_ALLOC(h->bnbrCnt, sizeof(int) * M);
-    SF_ALLOC(h->nbr, sizeof(unsigned) * M * kMaxNbr);
     SF_ALLOC(h->bnbr, sizeof(unsigned) * M * kMaxBNbr);
     SF_ALLOC(h->cnbrCnt, sizeof(int) * M);
     SF_ALLOC(h->cnbr, sizeof(unsigned) * M * kMaxContact);
@@ -517,6 +580,7 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
     SF_ALLOC(h->dBlockScene, sizeof(int) * blockScene.size());
     SF_ALLOC(h->dState, sizeof(SceneState) * n_scenes);
     SF_ALLOC(h->dErr, sizeof(unsigned));
+    SF_ALLOC(h->dProbe, sizeof(unsigned));
 #undef SF_ALLOC
     // host staging of the initial state
     std::vector<float4> hpos(M, make_float4(0, 0, 0, 0)), hvel(M, make_float4(0, 0, 0, 0)),
@@ -593,6 +657,8 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
     }
     if (h->cuda(cudaGetLastError(), "boundary volume") || h->cuda(cudaStreamSynchronize(h->stream), "create sync"))
         return bail(SF_ERR_CUDA);
+    // neighbour list capacity from the initial neighbour counts
+    if (probeListCapacity(h) != SF_OK) return bail(SF_ERR_CUDA);
     *out = h;
     return SF_OK;
 }
@@ -1041,8 +1107,65 @@ sf_status sf_launch_count(const sf_handle* h, int64_t* launches) {
 
 sf_status sf_set_tuning(sf_handle* h, int32_t block_size, int32_t items_per_thread) {
     if (!h) return SF_ERR_INVALID;
-    if ((block_size != 0 && block_size != kSlotAlign) || (items_per_thread != 0 && items_per_thread != 1))
-        return h->fail(SF_ERR_UNSUPPORTED, "this build runs the passes with 256 threads, one slot each");
+    if (items_per_thread != 0 && items_per_thread != 1)
+        return h->fail(SF_ERR_UNSUPPORTED, "the passes handle one particle slot per thread");
+    if (block_size == 0) return SF_OK;
+    if (block_size != 32 && block_size != 64 && block_size != 128 && block_size != 256)
+        return h->fail(SF_ERR_INVALID, "block_size must be 32, 64, 128 or 256");
+    for (int k = 0; k < kTunedPasses; ++k) h->block[k] = block_size;
+    h->dropGraphs();
+    return SF_OK;
+}
+
+sf_status sf_autotune(sf_handle* h, float dt, int32_t* block_sizes_out, int32_t* list_capacity_out) {
+    if (!h) return SF_ERR_INVALID;
+    if (!(dt > 0.f) || !std::isfinite(dt)) return h->fail(SF_ERR_INVALID, "dt must be finite and > 0");
+    sf_status st = SF_OK;
+    if (!h->sorted && (st = runSort(h))) return st;
+    if ((st = probeListCapacity(h))) return st;
+    if (h->slab) {  // stored-substep slabs depend on the list capacity
+        if (h->cuda(cudaStreamSynchronize(h->stream), "sync before slab release")) return SF_ERR_CUDA;
+        devFree(h->slab);
+        h->slabBytes = 0;
+    }
+    // every pass recomputes its outputs from inputs it does not write, so
+    // repeating it on the current state is harmless; the integrator is not
+    // repeated (it advances the state) and keeps its block size
+    const int candidates[3] = {64, 128, 256};
+    const int stages[kTunedPasses - 1] = {SF_STAGE_DENSITY, SF_STAGE_AVGFLOW, SF_STAGE_VOIDAGE_ADHESION,
+                                          SF_STAGE_SAND_MOMENTUM, SF_STAGE_WATER_MOMENTUM};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (h->cuda(cudaEventCreate(&e0), "event") || h->cuda(cudaEventCreate(&e1), "event")) return SF_ERR_CUDA;
+    for (int s = SF_STAGE_DENSITY; s <= SF_STAGE_WATER_MOMENTUM && st == SF_OK; ++s) st = runStage(h, s, dt, 0);
+    for (int p = 0; p < kTunedPasses - 1 && st == SF_OK; ++p) {
+        float best = 0.f;
+        int bestBs = h->block[p];
+        for (int bs : candidates) {
+            h->block[p] = bs;
+            if ((st = runStage(h, stages[p], dt, 0))) break;
+            cudaEventRecord(e0, h->stream);
+            for (int r = 0; r < 5 && st == SF_OK; ++r) st = runStage(h, stages[p], dt, 0);
+            cudaEventRecord(e1, h->stream);
+            float ms = 0.f;
+            if (st || h->cuda(cudaEventSynchronize(e1), "tune sync") ||
+                h->cuda(cudaEventElapsedTime(&ms, e0, e1), "tune time")) {
+                st = st ? st : SF_ERR_CUDA;
+                break;
+            }
+            if (best == 0.f || ms < best) {
+                best = ms;
+                bestBs = bs;
+            }
+        }
+        h->block[p] = bestBs;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st) return st;
+    h->dropGraphs();
+    if (block_sizes_out)
+        for (int k = 0; k < kTunedPasses; ++k) block_sizes_out[k] = h->block[k];
+    if (list_capacity_out) *list_capacity_out = h->nbrCap;
     return SF_OK;
 }
 
@@ -1078,7 +1201,7 @@ sf_status snapCopy(sf_handle* h, char* snap, bool save) {
 // One slab = what the adjoint of one substep reads (AdjSlab), 256-byte aligned.
 size_t slabStride(const sf_handle* h) {
     const size_t M = size_t(h->totalSlots);
-    const size_t b = M * (sizeof(unsigned) * (1 + kMaxNbr + kMaxContact) + sizeof(int) * 2 + sizeof(unsigned) * kMaxBNbr +
+    const size_t b = M * (sizeof(unsigned) * (1 + size_t(h->nbrCap) + kMaxContact) + sizeof(int) * 2 + sizeof(unsigned) * kMaxBNbr +
                           9 * sizeof(float4) + sizeof(int)) +
                      sizeof(unsigned) * (size_t(h->totalCells) + 1);
     return (b + 255) / 256 * 256;
@@ -1102,7 +1225,7 @@ AdjSlab slabAt(const sf_handle* h, char* base) {
     s.adh = reinterpret_cast<float4*>(take(sizeof(float4) * M));
     s.avgadh = reinterpret_cast<float4*>(take(sizeof(float4) * M));
     s.mat = reinterpret_cast<float4*>(take(sizeof(float4) * M));
-    s.nbr = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * M * kMaxNbr));
+    s.nbr = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * M * size_t(h->nbrCap)));
     s.bnbr = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * M * kMaxBNbr));
     s.cnbr = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * M * kMaxContact));
     s.cnt = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * M));
@@ -1123,7 +1246,7 @@ PassBuffers slabBuffers(const sf_handle* h, const AdjSlab& s) {
     b.lists.ccnt = s.ccnt;
     b.lists.cnbr = s.cnbr;
     b.lists.cs = s.cs;
-    b.listsW = NbrListsW{s.cnt, s.nbr, s.bcnt, s.bnbr, s.ccnt, s.cnbr, s.cs, h->bcs, b.lists.M};
+    b.listsW = NbrListsW{s.cnt, s.nbr, s.bcnt, s.bnbr, s.ccnt, s.cnbr, s.cs, h->bcs, b.lists.M, h->nbrCap};
     b.pos4 = s.pos;
     b.vel4 = s.vel;
     b.aux4 = s.aux;

@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(kSlotAlign) kDensity(const SceneDev* __restric
                     const unsigned j = j0 + unsigned(t);
                     const float4 pj = pos4[j];
                     const bool sandJ = pj.w < 0.f;
-                    if (cS + cW < kMaxNbr) nb[(sandJ ? cS : kMaxNbr - 1 - cW) * M] = j;
+                    if (cS + cW < L.cap) nb[(sandJ ? cS : L.cap - 1 - cW) * M] = j;
                     if (sandJ) {
                         ++cS;
                         if (!water && j != unsigned(slot)) {
@@ -578,7 +578,37 @@ __global__ void kIntegrate(const SceneDev* __restrict__ scenes, const int* __res
     avgadh4[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
+// ------------------------------------------------- neighbour-count probe
+// The list capacity probe: particles within the interaction reach of each
+// particle, walked like the density pass, maxed over all particles.
+__global__ void kNeighborCountMax(const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene,
+                                  const float4* __restrict__ pos4, const unsigned int* __restrict__ cs,
+                                  unsigned int* maxCount) {
+    SF_SLOT_PROLOGUE
+    const float4 pi4 = pos4[slot];
+    unsigned n = 0;
+    if (pi4.w != 0.f) {
+        const float3 pi = xyz(pi4);
+        const int3 c = cellOf(S, pi);
+        const int z0 = max(c.z - 1, 0), z1 = min(c.z + 1, S.gz - 1) + 1;
+        for (int x = max(c.x - 1, 0); x <= min(c.x + 1, S.gx - 1); ++x)
+            for (int y = max(c.y - 1, 0); y <= min(c.y + 1, S.gy - 1); ++y) {
+                const int base = S.cell_off + (x * S.gy + y) * S.gz;
+                for (unsigned j = cs[base + z0]; j < cs[base + z1]; ++j) n += inReachFast(S, pi - xyz(pos4[j])) ? 1u : 0u;
+            }
+    }
+    for (int o = 16; o > 0; o >>= 1) n = max(n, __shfl_xor_sync(0xffffffffu, n, o));
+    if ((threadIdx.x & 31) == 0 && n > 0) atomicMax(maxCount, n);
+}
+
 // ------------------------------------------------------------ launchers
+// Blocks of a tuned pass over all slots.
+static inline int grid(const LaunchCtx& c, int pass) { return c.slotBlocks * (kSlotAlign / c.block[pass]); }
+
+void launchNeighborCountMax(const LaunchCtx& c, const float4* pos4, const unsigned int* cs, unsigned int* maxCount) {
+    kNeighborCountMax<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, pos4, cs, maxCount);
+}
+
 void launchKeys(const LaunchCtx& c, const float4* pos4, unsigned int* keys) {
     kKeys<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, pos4, keys, c.errWord);
 }
@@ -590,34 +620,34 @@ void launchBoundaryVolume(const LaunchCtx& c, int sid, int nb, float4* bpos4, co
 }
 
 void launchDensity(const LaunchCtx& c, const PassBuffers& b) {
-    kDensity<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, c.state, b.listsW, b.pos4, b.bpos4,
+    kDensity<<<grid(c, kPassDensity), c.block[kPassDensity], 0, c.stream>>>(c.scenes, c.blockScene, c.state, b.listsW, b.pos4, b.bpos4,
                                                         b.vel4, b.aux4);
 }
 
 void launchAvgFlow(const LaunchCtx& c, const PassBuffers& b) {
-    kAvgFlow<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, b.lists, b.pos4, b.vel4, b.aux4,
+    kAvgFlow<<<grid(c, kPassAvgFlow), c.block[kPassAvgFlow], 0, c.stream>>>(c.scenes, c.blockScene, b.lists, b.pos4, b.vel4, b.aux4,
                                                         b.flow4);
 }
 
 void launchVoidageAdhesion(const LaunchCtx& c, const PassBuffers& b) {
-    kVoidageAdhesion<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, b.lists, b.pos4, b.vel4,
+    kVoidageAdhesion<<<grid(c, kPassVoidage), c.block[kPassVoidage], 0, c.stream>>>(c.scenes, c.blockScene, b.lists, b.pos4, b.vel4,
                                                                 b.aux4, b.adh4, b.avgadh4, b.col4);
 }
 
 void launchSandMomentum(const LaunchCtx& c, const PassBuffers& b) {
-    kSandMomentum<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, b.lists, b.pos4, b.vel4,
+    kSandMomentum<<<grid(c, kPassSand), c.block[kPassSand], 0, c.stream>>>(c.scenes, c.blockScene, b.lists, b.pos4, b.vel4,
                                                              b.aux4, b.flow4, b.avgadh4, b.mat4, b.bpos4, b.drag4,
                                                              b.acc4);
 }
 
 void launchWaterMomentum(const LaunchCtx& c, const PassBuffers& b) {
-    kWaterMomentum<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, c.state, b.lists, b.pos4,
+    kWaterMomentum<<<grid(c, kPassWater), c.block[kPassWater], 0, c.stream>>>(c.scenes, c.blockScene, c.state, b.lists, b.pos4,
                                                               b.vel4, b.aux4, b.drag4, b.adh4, b.bpos4, b.acc4,
                                                               c.errWord);
 }
 
 void launchIntegrate(const LaunchCtx& c, const PassBuffers& b, float timeArg, int adaptive) {
-    kIntegrate<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, c.state, timeArg, adaptive,
+    kIntegrate<<<grid(c, kPassIntegrate), c.block[kPassIntegrate], 0, c.stream>>>(c.scenes, c.blockScene, c.state, timeArg, adaptive,
                                                           b.lists.bcs, b.bpos4, b.pos4, b.vel4, b.acc4, b.adh4,
                                                           b.avgadh4);
 }

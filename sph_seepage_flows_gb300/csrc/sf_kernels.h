@@ -9,6 +9,10 @@ namespace sfg {
 struct SceneDev;
 struct SceneState;
 
+// Passes whose block size the tuner picks (threads per block, a divisor of
+// kSlotAlign so that a block never spans two scenes).
+enum TunedPass { kPassDensity = 0, kPassAvgFlow, kPassVoidage, kPassSand, kPassWater, kPassIntegrate, kTunedPasses };
+
 // Launch context shared by all passes of one handle.
 struct LaunchCtx {
     cudaStream_t stream;
@@ -17,15 +21,19 @@ struct LaunchCtx {
     SceneState* state;        // device array [n_scenes]
     unsigned int* errWord;    // device error word
     int slotBlocks;           // total slots / kSlotAlign
+    int block[kTunedPasses];  // threads per block of each tuned pass
 };
 
 // Neighbour lists of the current substep (column-major: entry k of slot i at
 // k * M + i). Particle lists hold sand neighbours from entry 0 upwards and
-// water neighbours from entry kMaxNbr - 1 downwards; cnt packs the two counts
+// water neighbours from entry cap - 1 downwards; cnt packs the two counts
 // (sand in the low 16 bits, each saturating at 0xFFFF). Counts summing above
-// kMaxNbr mean the list overflowed: walk the stencil instead. A boundary count
-// above kMaxBNbr means the same for the boundary list.
-constexpr int kMaxNbr = 64;
+// cap mean the list overflowed: walk the stencil instead. A boundary count
+// above kMaxBNbr means the same for the boundary list. The capacity cap is
+// chosen per handle from the neighbour counts of its scenes (a multiple of
+// 32 between kMinNbr and kMaxNbr).
+constexpr int kMinNbr = 64;
+constexpr int kMaxNbr = 256;
 constexpr int kMaxBNbr = 48;
 // Sand-sand pairs within DEM contact + liquid-bridge reach of a sand particle
 // (the only pairs with DEM or capillary forces); more means "filter the sand list".
@@ -40,6 +48,7 @@ struct NbrLists {
     const unsigned int* cs;   // particle cell table (total_cells + 1)
     const unsigned int* bcs;  // boundary cell table (total_cells + 1)
     long long M;              // total slots
+    int cap;                  // particle list capacity
 };
 struct NbrListsW {
     unsigned int* cnt;
@@ -51,6 +60,7 @@ struct NbrListsW {
     const unsigned int* cs;
     const unsigned int* bcs;
     long long M;
+    int cap;
 };
 
 // Device buffers the neighbor passes read and write (current sort order).
@@ -79,6 +89,9 @@ void launchVoidageAdhesion(const LaunchCtx& c, const PassBuffers& b);
 void launchSandMomentum(const LaunchCtx& c, const PassBuffers& b);
 void launchWaterMomentum(const LaunchCtx& c, const PassBuffers& b);
 void launchIntegrate(const LaunchCtx& c, const PassBuffers& b, float timeArg, int adaptive);
+// Largest number of particles within the interaction reach of any particle
+// (itself included), atomically maxed into *maxCount; needs the cell table.
+void launchNeighborCountMax(const LaunchCtx& c, const float4* pos4, const unsigned int* cs, unsigned int* maxCount);
 
 // ---- stable LSD radix sort of 32-bit cell keys (sf_sort.cu) ----
 // Scratch sizes for sorting n keys.

@@ -39,9 +39,9 @@ template <bool kSand, typename F>
 __device__ __forceinline__ void forLabelNeighbors(const SceneDev& S, const NbrLists& L, int slot, float3 pi,
                                                   const float4* __restrict__ pos4, F&& f) {
     const unsigned c = L.cnt[slot];
-    if (int(c & 0xFFFFu) + int(c >> 16) <= kMaxNbr) {
+    if (int(c & 0xFFFFu) + int(c >> 16) <= L.cap) {
         const int n = kSand ? int(c & 0xFFFFu) : int(c >> 16);
-        const unsigned* __restrict__ p = L.nbr + slot + (kSand ? 0 : size_t(kMaxNbr - 1) * L.M);
+        const unsigned* __restrict__ p = L.nbr + slot + (kSand ? 0 : size_t(L.cap - 1) * L.M);
         const long long step = kSand ? L.M : -L.M;
         // indices are loaded a group ahead so the neighbour gathers of
         // consecutive entries overlap

@@ -311,6 +311,82 @@ def adjoint_column(seed: int = 5) -> Scene:
                        sand_origin=(0.29, 0.02, 0.29), water_origin=(0.1, 0.02, 0.1))
 
 
+def column_scene(name: str, n_sand: int, n_water: int, seed: int, pitch: float = 0.02) -> Scene:
+    """Column collapse: a sand column (height twice its width) in the middle
+    of a square box whose base is flooded by a water layer three particles
+    deep, the lattices offset by half a pitch (the adjoint-column geometry at
+    another size)."""
+    r = pitch / 2.0
+    params = reference_params(sph_radius=r, dem_radius=r)
+    s = max(2, int(round((n_sand / 2.0) ** (1.0 / 3.0))))
+    sand_counts = (s, max(2, int(round(n_sand / (s * s)))), s)
+    w = max(2, int(round(math.sqrt(n_water / 3.0))))
+    water_counts = (w, 3, w)
+    side = (max(w, s) + 4) * pitch
+    height = (sand_counts[1] + 4) * pitch
+    box = (float(np.float32(side)), float(np.float32(height)), float(np.float32(side)))
+    bparams = boundary_params((0.0, 0.0, 0.0), box, params.sph_kernel_radius)
+    rng = np.random.default_rng(seed)
+    sand = _lattice((0.5 * side - 0.5 * (s - 1) * pitch, pitch, 0.5 * side - 0.5 * (s - 1) * pitch), sand_counts,
+                    pitch, rng, 0.01)
+    wo = 0.5 * side - 0.5 * (w - 1) * pitch + 0.5 * pitch
+    water = _lattice((wo, pitch, wo), water_counts, pitch, rng, 0.01)
+    return _assemble(name, params, bparams, solver_params(), sand, water, r, r,
+                     meta={"seed": seed, "geometry": "column", "sand_counts": list(sand_counts),
+                           "water_counts": list(water_counts)})
+
+
+def embankment_scene(name: str, n_sand: int, n_water: int, seed: int, pitch: float = 0.02) -> Scene:
+    """Embankment seepage: a sand trapezoid (1V:2H slopes, 10 layers high)
+    with the reservoir behind it to 80% of its height, the depth (z extent)
+    chosen for the sand count and the reservoir length for the water count."""
+    r = pitch / 2.0
+    params = reference_params(sph_radius=r, dem_radius=r)
+    height = 10 * pitch
+    level = 0.8 * height
+    y0 = 2.0 * r
+    crest = 4 * pitch
+    toe_rel = lambda L: 2.0 * r + L  # noqa: E731
+    per_z = _rows_count(_embankment_rows(0.0, crest, height, pitch, y0), 1)
+    nz = max(2, int(round(n_sand / per_z)))
+    lo_L, hi_L = 0.0, 20.0
+    for _ in range(50):
+        mid = 0.5 * (lo_L + hi_L)
+        if _rows_count(_reservoir_rows(2.0 * r, toe_rel(mid), level, pitch, y0, pitch), nz) < n_water:
+            lo_L = mid
+        else:
+            hi_L = mid
+    toe = toe_rel(hi_L)
+    length = toe + crest + 4.0 * height + 4.0 * pitch
+    depth = (nz + 3) * pitch
+    box = (float(np.float32(length)), float(np.float32(height + 4 * pitch)), float(np.float32(depth)))
+    bparams = boundary_params((0.0, 0.0, 0.0), box, params.sph_kernel_radius)
+    zs_s = _axis(2.0 * 2.0 * r, 2.0 * 2.0 * r + (nz - 1) * pitch, pitch)   # the z-min wall tests 2 * rij
+    zs_w = zs_s
+    rng = np.random.default_rng(seed)
+    sand = _rows_points(_embankment_rows(toe, crest, height, pitch, y0), zs_s)
+    water = _rows_points(_reservoir_rows(2.0 * r, toe, level, pitch, y0, pitch), zs_w)
+    sand = (sand + rng.uniform(-0.01 * pitch, 0.01 * pitch, size=sand.shape)).astype(np.float32)
+    water = (water + rng.uniform(-0.01 * pitch, 0.01 * pitch, size=water.shape)).astype(np.float32)
+    return _assemble(name, params, bparams, solver_params(), sand, water, r, r,
+                     meta={"seed": seed, "geometry": "embankment", "toe": toe, "depth_layers": nz})
+
+
+def calibration_scenes(n_scenes: int = 32, seed: int = 77, n_min: int = 10_000, n_max: int = 50_000):
+    """Scenes of the batched calibration: sizes log-uniform in [n_min, n_max],
+    sand fraction U[0.4, 0.6], alternating column-collapse and
+    embankment-seepage geometries."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for s in range(n_scenes):
+        n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
+        frac = rng.uniform(0.4, 0.6)
+        ns, nw = int(round(n * frac)), n - int(round(n * frac))
+        make = column_scene if s % 2 == 0 else embankment_scene
+        out.append(make(f"calib_{s:02d}", ns, nw, seed * 1000 + s))
+    return out
+
+
 def capillary_rupture(r: float) -> float:
     """Liquid-bridge rupture distance of two sand spheres of radius r
     (ComputeDemCapillaryForces, cuda_dem_solver_common_gpu.cuh:63-65)."""

@@ -1,0 +1,62 @@
+"""Launch tuning (sf_set_tuning, sf_autotune) changes speed, never results:
+every pass computes each slot's outputs independently of the block shape,
+so substeps run with any block size are bit-identical. The list capacity
+probe sizes the neighbour lists so dense scenes do not overflow them."""
+
+import numpy as np
+import pytest
+
+from sph_seepage_flows_gb300 import scenes
+from sph_seepage_flows_gb300.params import reference_dt
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["pos", "vel", "acc", "density", "pressure", "voidage", "saturation", "avg_flow", "avg_drag",
+          "adhesion", "avg_adhesion", "col"]
+
+
+def run(sc, tune):
+    from sph_seepage_flows_gb300.capi import Simulation
+    sim = Simulation(sc)
+    dt = reference_dt(sc.params, sc.bparams, sc.sparams)[1]
+    info = tune(sim, dt)
+    sim.substeps_fixed(dt, 4)
+    out = {f: sim.field(f, order="id") for f in FIELDS}
+    sim.close()
+    return out, info
+
+
+@pytest.mark.parametrize("name", ["tiny", "plain_small"])
+def test_block_size_does_not_change_results(cuda_lib, name):
+    sc = getattr(scenes, name)()
+    ref, _ = run(sc, lambda s, dt: None)
+    for bs in (32, 64, 128):
+        out, _ = run(sc, lambda s, dt: s.set_tuning(bs))
+        for f in FIELDS:
+            assert np.array_equal(out[f], ref[f]), (bs, f)
+    out, info = run(sc, lambda s, dt: s.autotune(dt))
+    assert set(info["block_sizes"].values()) <= {64, 128, 256}
+    for f in FIELDS:
+        assert np.array_equal(out[f], ref[f]), ("autotune", f)
+
+
+def test_list_capacity_covers_dense_scene(cuda_lib):
+    from sph_seepage_flows_gb300.capi import Simulation
+    sc = scenes.adjoint_column()   # interpenetrating sand / water base: up to ~70 neighbours
+    sim = Simulation(sc)
+    dt = reference_dt(sc.params, sc.bparams, sc.sparams)[1]
+    info = sim.autotune(dt)
+    sim.stage("sort")
+    sim.stage("density")
+    nb = sim.field("neighbors")
+    assert info["list_capacity"] % 32 == 0 and info["list_capacity"] >= nb.max() > 64
+
+
+def test_set_tuning_rejects_bad_sizes(cuda_lib):
+    from sph_seepage_flows_gb300.capi import SfError, Simulation
+    sim = Simulation(scenes.tiny())
+    for bad in (100, 512, -1):
+        with pytest.raises(SfError):
+            sim.set_tuning(bad)
+    with pytest.raises(SfError):
+        sim.set_tuning(64, 2)
