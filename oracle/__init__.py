@@ -131,6 +131,10 @@ def _load_oracle():
     lib.sfo_set_threads.argtypes = [ctypes.c_int]
     lib.sfo_interaction_reach.restype = ctypes.c_double
     lib.sfo_interaction_reach.argtypes = [ctypes.POINTER(SfParams), ctypes.POINTER(SfBoundaryParams)]
+    for name in ("sfo_set_tangent", "sfo_get_tangent"):
+        getattr(lib, name).argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                       ctypes.c_int64]
+    lib.sfo_seed_param.argtypes = [ctypes.c_void_p, ctypes.c_int]
     return lib
 
 
@@ -150,7 +154,10 @@ def set_threads(n: int) -> int:
 
 class Oracle(_Base):
     """CPU restatement of one scene. precision 32 = reference FP32 arithmetic,
-    64 = the FP64 yardstick. sort_multi selects SearcherParticleType."""
+    64 = the FP64 yardstick, 65 = FP64 carrying one forward-mode tangent (exact
+    pathwise directional derivatives). sort_multi selects SearcherParticleType."""
+
+    PARAMS = {"none": 0, "tan": 1, "cap": 2, "perm": 3}
 
     _prefix = "sfo_"
 
@@ -169,6 +176,28 @@ class Oracle(_Base):
                                      ctypes.c_int64(self.n))
         if rc != 0:
             raise RuntimeError(f"set_field({name}) failed")
+
+    def set_tangent(self, name: str, values) -> None:
+        """Tangent of positions or velocities (precision 65), internal order."""
+        fid, _, _ = _field_meta(name)
+        a = np.ascontiguousarray(np.asarray(values, dtype=np.float64).reshape(-1))
+        if self._lib.sfo_set_tangent(self.h, fid, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                     ctypes.c_int64(self.n)) != 0:
+            raise RuntimeError(f"set_tangent({name}) failed")
+
+    def tangent(self, name: str) -> np.ndarray:
+        fid, _, _ = _field_meta(name)
+        out = np.zeros(3 * self.n, dtype=np.float64)
+        if self._lib.sfo_get_tangent(self.h, fid, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                     ctypes.c_int64(self.n)) != 0:
+            raise RuntimeError(f"tangent({name}) failed")
+        return out.reshape(self.n, 3)
+
+    def seed_param(self, which: str) -> None:
+        """Differentiate by 'tan' (tan friction angle), 'cap' (capillary scale),
+        'perm' (permeability scale) or 'none' (precision 65)."""
+        if self._lib.sfo_seed_param(self.h, self.PARAMS[which]) != 0:
+            raise RuntimeError("seed_param failed")
 
     def stage(self, name, time_arg: float = 0.0, adaptive: bool = False) -> None:
         sid = STAGE_ID[name] if isinstance(name, str) else int(name)

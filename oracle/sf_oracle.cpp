@@ -33,12 +33,84 @@
 #include <cstdint>
 #include <cstring>
 #include <limits>
+#include <type_traits>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
 
 namespace sfo {
+
+// Forward-mode dual number: an FP64 value and one tangent. Sim<Dual1> runs
+// the FP64 restatement while carrying the derivative of every quantity
+// along one direction (initial positions / velocities or one parameter), the
+// exact pathwise directional derivative that a reverse-mode gradient must
+// reproduce. Comparisons and branches use the value.
+struct Dual1 {
+    double v = 0.0, d = 0.0;
+    Dual1() = default;
+    Dual1(double x) : v(x), d(0.0) {}  // NOLINT: constants convert implicitly
+    Dual1(double x, double t) : v(x), d(t) {}
+    explicit operator double() const { return v; }
+    explicit operator float() const { return float(v); }
+    explicit operator int() const { return int(v); }
+    explicit operator long() const { return long(v); }
+    explicit operator long long() const { return (long long)(v); }
+    Dual1& operator+=(Dual1 b) { v += b.v; d += b.d; return *this; }
+    Dual1& operator-=(Dual1 b) { v -= b.v; d -= b.d; return *this; }
+    Dual1& operator*=(Dual1 b) { d = d * b.v + v * b.d; v *= b.v; return *this; }
+    Dual1& operator/=(Dual1 b) { const double q = v / b.v; d = (d - q * b.d) / b.v; v = q; return *this; }
+};
+inline Dual1 operator+(Dual1 a, Dual1 b) { return Dual1(a.v + b.v, a.d + b.d); }
+inline Dual1 operator-(Dual1 a, Dual1 b) { return Dual1(a.v - b.v, a.d - b.d); }
+inline Dual1 operator-(Dual1 a) { return Dual1(-a.v, -a.d); }
+inline Dual1 operator*(Dual1 a, Dual1 b) { return Dual1(a.v * b.v, a.d * b.v + a.v * b.d); }
+inline Dual1 operator/(Dual1 a, Dual1 b) { const double q = a.v / b.v; return Dual1(q, (a.d - q * b.d) / b.v); }
+inline bool operator<(Dual1 a, Dual1 b) { return a.v < b.v; }
+inline bool operator>(Dual1 a, Dual1 b) { return a.v > b.v; }
+inline bool operator<=(Dual1 a, Dual1 b) { return a.v <= b.v; }
+inline bool operator>=(Dual1 a, Dual1 b) { return a.v >= b.v; }
+inline bool operator==(Dual1 a, Dual1 b) { return a.v == b.v; }
+inline bool operator!=(Dual1 a, Dual1 b) { return a.v != b.v; }
+
+// Math functions of the restatement: the std functions for float / double,
+// their derivatives for Dual1.
+inline float tsqrt(float x) { return std::sqrt(x); }
+inline double tsqrt(double x) { return std::sqrt(x); }
+inline Dual1 tsqrt(Dual1 a) {
+    const double r = std::sqrt(a.v);
+    return Dual1(r, r > 0.0 ? a.d / (2.0 * r) : 0.0);
+}
+inline float tpow(float a, float b) { return std::pow(a, b); }
+inline double tpow(double a, double b) { return std::pow(a, b); }
+inline Dual1 tpow(Dual1 a, Dual1 b) {
+    const double r = std::pow(a.v, b.v);
+    double d = a.v != 0.0 ? b.v * std::pow(a.v, b.v - 1.0) * a.d : 0.0;
+    if (b.d != 0.0 && a.v > 0.0) d += std::log(a.v) * r * b.d;
+    return Dual1(r, d);
+}
+inline float tfmax(float a, float b) { return std::fmax(a, b); }
+inline double tfmax(double a, double b) { return std::fmax(a, b); }
+inline Dual1 tfmax(Dual1 a, Dual1 b) { return (a.v > b.v || b.v != b.v) ? a : b; }
+inline float tfmin(float a, float b) { return std::fmin(a, b); }
+inline double tfmin(double a, double b) { return std::fmin(a, b); }
+inline Dual1 tfmin(Dual1 a, Dual1 b) { return (a.v < b.v || b.v != b.v) ? a : b; }
+inline float tfabs(float x) { return std::fabs(x); }
+inline double tfabs(double x) { return std::fabs(x); }
+inline Dual1 tfabs(Dual1 a) { return a.v < 0.0 ? -a : a; }
+inline float tcos(float x) { return std::cos(x); }
+inline double tcos(double x) { return std::cos(x); }
+inline Dual1 tcos(Dual1 a) { return Dual1(std::cos(a.v), -std::sin(a.v) * a.d); }
+inline float tsin(float x) { return std::sin(x); }
+inline double tsin(double x) { return std::sin(x); }
+inline Dual1 tsin(Dual1 a) { return Dual1(std::sin(a.v), std::cos(a.v) * a.d); }
+
+// A parameter value, carrying the tangent t when T is Dual1.
+template <typename T> inline T seeded(float v, double t) {
+    (void)t;
+    return T(v);
+}
+template <> inline Dual1 seeded<Dual1>(float v, double t) { return Dual1(double(v), t); }
 
 // KIRI_EPSILON and KIRI_PI (seepage_flows_cuda/include/kiri_pbs_cuda/kiri_pbs_pch.cuh:52-54).
 template <typename T> constexpr T kEps() { return T(1e-6f); }
@@ -59,10 +131,10 @@ template <typename T> inline V3<T> operator/(V3<T> a, T s) { return mk(a.x / s, 
 template <typename T> inline void operator+=(V3<T>& a, V3<T> b) { a.x += b.x; a.y += b.y; a.z += b.z; }
 // helper_math.h dot / length / lengthSquared (cuda_helper/helper_math.h:1277-1323, math/cuda_math_utils.cuh:74)
 template <typename T> inline T dot(V3<T> a, V3<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-template <typename T> inline T length(V3<T> v) { return std::sqrt(dot(v, v)); }
+template <typename T> inline T length(V3<T> v) { return tsqrt(dot(v, v)); }
 template <typename T> inline T lengthSquared(V3<T> v) { return dot(v, v); }
-template <typename T> inline T tmax(T a, T b) { return std::fmax(a, b); }
-template <typename T> inline T tmin(T a, T b) { return std::fmin(a, b); }
+template <typename T> inline T tmax(T a, T b) { return tfmax(a, b); }
+template <typename T> inline T tmin(T a, T b) { return tfmin(a, b); }
 // sgn (math/cuda_math_utils.cuh:77-82): int in {-1,0,1}, converted back to T
 template <typename T> inline T sgnT(T v) { return T(int(T(0) < v) - int(v < T(0))); }
 
@@ -103,9 +175,9 @@ template <typename T> struct SpikyGrad {
 // AdhesionAkinci13 (KERN:189-203)
 template <typename T> struct Adhesion {
     T coef, h;
-    explicit Adhesion(T radius) : h(radius) { coef = T(0.007f) / std::pow(h, T(3.25f)); }
+    explicit Adhesion(T radius) : h(radius) { coef = T(0.007f) / tpow(h, T(3.25f)); }
     T operator()(T r) const {
-        if (T(2) * r > h && r <= h) return coef * std::pow(T(-4) * r * r / h + T(6) * r - T(2) * h, T(0.25f));
+        if (T(2) * r > h && r <= h) return coef * tpow(T(-4) * r * r / h + T(6) * r - T(2) * h, T(0.25f));
         return T(0);
     }
 };
@@ -121,7 +193,7 @@ template <typename T> struct Bezier {
         d = T(-4) * (T(1) + b - px1);
         e = T(2) * (T(1) + b - px1);
     }
-    T rx2t(T sr) const { return (b + std::sqrt(c + d * (px1 - sr))) / e; }
+    T rx2t(T sr) const { return (b + tsqrt(c + d * (px1 - sr))) / e; }
     T operator()(T sr) const {
         if (sr < T(0)) return py0;
         if (sr >= T(1)) return py2;
@@ -147,9 +219,9 @@ template <typename T> V3<T> demForce(V3<T> dij, V3<T> vij, T rij, T kn, T ks, T 
         V3<T> vt = vij - dot_e * n;
         V3<T> fn = kn * pen * n;
         V3<T> fs = -ks * vt;
-        T max_fs = lengthSquared(fn) * std::pow(tanFrictionAngle, T(2));
+        T max_fs = lengthSquared(fn) * tpow(tanFrictionAngle, T(2));
         if (lengthSquared(fs) > max_fs) {
-            T ratio = std::sqrt(max_fs) / length(fs);
+            T ratio = tsqrt(max_fs) / length(fs);
             fs = fs * ratio;
         }
         f = -fn - fs;
@@ -161,18 +233,18 @@ template <typename T> V3<T> demForce(V3<T> dij, V3<T> vij, T rij, T kn, T ks, T 
 template <typename T> V3<T> capillaryForce(V3<T> dij, T radiusi, T sr, const Bezier<T>& G) {
     V3<T> f = mk(T(0), T(0), T(0));
     T contact_angle = T(30) / T(180) * kPi<T>();
-    T vlb = T(4) / T(3) * kPi<T>() * std::pow(radiusi, T(3)) * T(0.01f) * T(0.01f);
+    T vlb = T(4) / T(3) * kPi<T>() * tpow(radiusi, T(3)) * T(0.01f) * T(0.01f);
     T s_rupture = (T(1) + T(0.5f) * contact_angle) *
-                  (std::pow(vlb, T(1.f / 3.f)) + T(0.1f) * std::pow(vlb, T(2.f / 3.f)));
+                  (tpow(vlb, T(1.f / 3.f)) + T(0.1f) * tpow(vlb, T(2.f / 3.f)));
     T dist = length(dij);
     T H = dist - (radiusi + radiusi);
     if (H < s_rupture && H > T(0)) {
         V3<T> N = dij / dist;
         T coeff_c = G(sr);
-        T d = -H + std::sqrt(H * H + vlb / (kPi<T>() * radiusi));
-        T phi = std::sqrt(T(2) * H / radiusi * (T(-1) + std::sqrt(T(1) + vlb / (kPi<T>() * radiusi * H * H))));
-        T ncp = T(-2) * kPi<T>() * coeff_c * radiusi * std::cos(contact_angle) / (T(1) + H / (T(2) * d));
-        T stf = T(-2) * kPi<T>() * coeff_c * radiusi * phi * std::sin(contact_angle);
+        T d = -H + tsqrt(H * H + vlb / (kPi<T>() * radiusi));
+        T phi = tsqrt(T(2) * H / radiusi * (T(-1) + tsqrt(T(1) + vlb / (kPi<T>() * radiusi * H * H))));
+        T ncp = T(-2) * kPi<T>() * coeff_c * radiusi * tcos(contact_angle) / (T(1) + H / (T(2) * d));
+        T stf = T(-2) * kPi<T>() * coeff_c * radiusi * phi * tsin(contact_angle);
         f = -N * (ncp + stf);
     }
     return f;
@@ -182,9 +254,9 @@ template <typename T> V3<T> capillaryForce(V3<T> dij, T radiusi, T sr, const Bez
 // to skip pairs whose every term is exactly zero (the reference adds +0 there).
 template <typename T> T capillaryReach(T radiusi) {
     T contact_angle = T(30) / T(180) * kPi<T>();
-    T vlb = T(4) / T(3) * kPi<T>() * std::pow(radiusi, T(3)) * T(0.01f) * T(0.01f);
+    T vlb = T(4) / T(3) * kPi<T>() * tpow(radiusi, T(3)) * T(0.01f) * T(0.01f);
     T s_rupture = (T(1) + T(0.5f) * contact_angle) *
-                  (std::pow(vlb, T(1.f / 3.f)) + T(0.1f) * std::pow(vlb, T(2.f / 3.f)));
+                  (tpow(vlb, T(1.f / 3.f)) + T(0.1f) * tpow(vlb, T(2.f / 3.f)));
     return T(2) * radiusi + s_rupture;
 }
 
@@ -218,6 +290,13 @@ template <typename T> struct Sim {
     // ---- solver state ----
     int64_t numSub = 1;
     T maxAccLen = 0;
+    // parameter whose tangent is seeded (Sim<Dual1>): 0 none, 1 tan friction
+    // angle, 2 capillary scale (factor on c0, cmc, csat), 3 permeability scale
+    // (factor on cd)
+    int seedParam = 0;
+    T param(float v, int which, bool relative) const {
+        return seeded<T>(v, which != 0 && which == seedParam ? (relative ? double(v) : 1.0) : 0.0);
+    }
 
     static T f2t(float v) { return T(v); }
     V3<T> f3(const float* v) const { return mk(T(v[0]), T(v[1]), T(v[2])); }
@@ -424,7 +503,7 @@ template <typename T> struct Sim {
             if (label[i] == 0) {
                 T p;
                 if (tait) {
-                    T x7 = std::pow(density[i] / rho0, T(7));
+                    T x7 = tpow(density[i] / rho0, T(7));
                     p = stiff * (x7 - T(1));
                     pressureScale[i] = stiff * x7;
                 } else {
@@ -565,10 +644,11 @@ template <typename T> struct Sim {
     void sandMomentumPass() {
         Poly6<T> W(cell);
         SpikyGrad<T> nablaW(cell);
-        Bezier<T> Gc(T(P.sf_c0), T(P.sf_cmc), T(P.sf_cmc_p), T(P.sf_csat));  // SOLV.cu:249,308
+        Bezier<T> Gc(param(P.sf_c0, 2, true), param(P.sf_cmc, 2, true), T(P.sf_cmc_p),
+                     param(P.sf_csat, 2, true));  // SOLV.cu:249,308
         const T radius_ = T(P.dem_particle_radius), waterRadius = T(P.sph_particle_radius);
-        const T young = T(P.dem_young), poisson = T(P.dem_poisson), tanF = T(P.dem_tan_friction_angle);
-        const T gravity = T(std::fabs(P.gravity[1]));  // abs(params.gravity.y), cuda_wcsph_sf_solver.cpp:106,136
+        const T young = T(P.dem_young), poisson = T(P.dem_poisson), tanF = param(P.dem_tan_friction_angle, 1, false);
+        const T gravity = T(tfabs(P.gravity[1]));  // abs(params.gravity.y), cuda_wcsph_sf_solver.cpp:106,136
         const T rho0 = T(P.sph_density);
         const bool multi = P.sf_type == SF_TYPE_MULTI_SF;
 #pragma omp parallel for schedule(dynamic, 256)
@@ -634,18 +714,18 @@ template <typename T> struct Sim {
                 T kn = young * radius_;
                 T ks = kn * poisson;
                 auto wall = [&](V3<T> N, T diff) { addf(demForce(N * diff, -vi, rij, kn, ks, tanF)); };
-                if (pi.x > hp.x - rij) wall(mk(T(1), T(0), T(0)), std::fabs(pi.x - hp.x));
-                if (pi.x < lp.x + rij) wall(mk(T(-1), T(0), T(0)), std::fabs(pi.x - lp.x));
-                if (pi.y > hp.y - rij) wall(mk(T(0), T(1), T(0)), std::fabs(pi.y - hp.y));
-                if (pi.y < lp.y + rij) wall(mk(T(0), T(-1), T(0)), std::fabs(pi.y - lp.y));
-                if (pi.z > hp.z - rij) wall(mk(T(0), T(0), T(1)), std::fabs(pi.z - hp.z));
-                if (pi.z < lp.z + T(2) * rij) wall(mk(T(0), T(0), T(-1)), std::fabs(pi.z - lp.z));
+                if (pi.x > hp.x - rij) wall(mk(T(1), T(0), T(0)), tfabs(pi.x - hp.x));
+                if (pi.x < lp.x + rij) wall(mk(T(-1), T(0), T(0)), tfabs(pi.x - lp.x));
+                if (pi.y > hp.y - rij) wall(mk(T(0), T(1), T(0)), tfabs(pi.y - hp.y));
+                if (pi.y < lp.y + rij) wall(mk(T(0), T(-1), T(0)), tfabs(pi.y - lp.y));
+                if (pi.z > hp.z - rij) wall(mk(T(0), T(0), T(1)), tfabs(pi.z - hp.z));
+                if (pi.z < lp.z + T(2) * rij) wall(mk(T(0), T(0), T(-1)), tfabs(pi.z - lp.z));
             }
             if (voidage[i] < T(1) && voidage[i] > T(0)) {
-                T cd = multi ? cda0asat[i].x : T(P.sf_cd);
-                T dragCoeff = cd * std::pow(voidage[i], T(3)) / std::pow(T(1) - voidage[i], T(2));
+                T cd = multi ? cda0asat[i].x : param(P.sf_cd, 3, true);
+                T dragCoeff = cd * tpow(voidage[i], T(3)) / tpow(T(1) - voidage[i], T(2));
                 if (dragCoeff != T(0))
-                    df = gravity * rho0 * std::pow(voidage[i], T(2)) / dragCoeff * (avgFlow[i] - vel[i]) * mass[i] /
+                    df = gravity * rho0 * tpow(voidage[i], T(2)) / dragCoeff * (avgFlow[i] - vel[i]) * mass[i] /
                          density[i];
             }
             avgDrag[i] = v_w != T(0) ? df / v_w : mk(T(0), T(0), T(0));
@@ -745,7 +825,7 @@ template <typename T> struct Sim {
         if (P.solver_type == SF_SOLVER_WCSPH) {
             T maxForce = bestLen * m;
             T bySpeed = T(0.4f) * h / T(S.speed_of_sound);
-            T byForce = T(0.25f) * std::sqrt(h * m / maxForce);
+            T byForce = T(0.25f) * tsqrt(h * m / maxForce);
             T desired = tmin(T(S.time_step_limit_scale) * tmin(bySpeed, byForce), T(P.dt));
             numSub = int64_t(renderInterval / desired);
         } else {
@@ -847,10 +927,34 @@ template <typename T> struct Sim {
 };
 
 struct Handle {
-    int precision;
+    int precision;  // 32, 64, or 65 = FP64 with one forward-mode tangent
     Sim<float> f;
     Sim<double> d;
+    Sim<Dual1> j;
+    template <typename F> auto visit(F&& fn) {
+        if (precision == 65) return fn(j);
+        if (precision == 64) return fn(d);
+        return fn(f);
+    }
 };
+
+// Tangents (Sim<Dual1>) of positions or velocities, in the current internal order.
+inline int tangentField(Sim<Dual1>& s, int field, double* get, const double* set, int64_t count) {
+    if (count != s.n || (field != SF_FIELD_POS && field != SF_FIELD_VEL)) return SF_ERR_INVALID;
+    std::vector<V3<Dual1>>& a = field == SF_FIELD_POS ? s.pos : s.vel;
+    for (int64_t i = 0; i < s.n; ++i) {
+        if (set) {
+            a[i].x.d = set[3 * i];
+            a[i].y.d = set[3 * i + 1];
+            a[i].z.d = set[3 * i + 2];
+        } else {
+            get[3 * i] = a[i].x.d;
+            get[3 * i + 1] = a[i].y.d;
+            get[3 * i + 2] = a[i].z.d;
+        }
+    }
+    return SF_OK;
+}
 
 template <typename T> int getField(Sim<T>& s, int field, double* dst, int64_t count) {
     const int64_t n = (field >= SF_BFIELD_POS && field < 100) ? s.nb : s.n;
@@ -951,96 +1055,108 @@ extern "C" {
 void* sfo_create(int precision, const sf_params* p, const sf_boundary_params* b, const sf_solver_params* s,
                  const sf_scene_init* in, int sort_multi) {
     auto* h = new sfo::Handle();
-    h->precision = precision == 64 ? 64 : 32;
-    if (h->precision == 64)
-        h->d.init(p, b, s, in, sort_multi);
-    else
-        h->f.init(p, b, s, in, sort_multi);
+    h->precision = (precision == 64 || precision == 65) ? precision : 32;
+    h->visit([&](auto& sim) {
+        sim.init(p, b, s, in, sort_multi);
+        return 0;
+    });
     return h;
 }
 
 void sfo_destroy(void* hv) { delete static_cast<sfo::Handle*>(hv); }
 
 int sfo_size(void* hv, int64_t* n, int64_t* nb) {
-    auto* h = static_cast<sfo::Handle*>(hv);
-    *n = h->precision == 64 ? h->d.n : h->f.n;
-    *nb = h->precision == 64 ? h->d.nb : h->f.nb;
-    return SF_OK;
+    return static_cast<sfo::Handle*>(hv)->visit([&](auto& sim) {
+        *n = sim.n;
+        *nb = sim.nb;
+        return int(SF_OK);
+    });
 }
 
 int sfo_get_field(void* hv, int field, double* dst, int64_t count) {
-    auto* h = static_cast<sfo::Handle*>(hv);
-    return h->precision == 64 ? sfo::getField(h->d, field, dst, count) : sfo::getField(h->f, field, dst, count);
+    return static_cast<sfo::Handle*>(hv)->visit([&](auto& sim) { return sfo::getField(sim, field, dst, count); });
 }
 
 int sfo_set_field(void* hv, int field, const double* src, int64_t count) {
-    auto* h = static_cast<sfo::Handle*>(hv);
-    return h->precision == 64 ? sfo::setField(h->d, field, src, count) : sfo::setField(h->f, field, src, count);
+    return static_cast<sfo::Handle*>(hv)->visit([&](auto& sim) { return sfo::setField(sim, field, src, count); });
 }
 
 // which: 0 = particle cell table, 1 = boundary cell table (G+1 entries)
 int sfo_get_cell_table(void* hv, int which, int64_t* dst, int64_t count) {
-    auto* h = static_cast<sfo::Handle*>(hv);
-    const std::vector<int64_t>& t = h->precision == 64 ? (which ? h->d.bcellStart : h->d.cellStart)
-                                                        : (which ? h->f.bcellStart : h->f.cellStart);
-    if (count != int64_t(t.size())) return SF_ERR_INVALID;
-    std::memcpy(dst, t.data(), sizeof(int64_t) * t.size());
-    return SF_OK;
+    return static_cast<sfo::Handle*>(hv)->visit([&](auto& sim) {
+        const std::vector<int64_t>& t = which ? sim.bcellStart : sim.cellStart;
+        if (count != int64_t(t.size())) return int(SF_ERR_INVALID);
+        std::memcpy(dst, t.data(), sizeof(int64_t) * t.size());
+        return int(SF_OK);
+    });
 }
 
 int sfo_run_stage(void* hv, int stage, double time_arg, int adaptive) {
-    auto* h = static_cast<sfo::Handle*>(hv);
     if (stage < 0 || stage >= SF_STAGE_COUNT) return SF_ERR_INVALID;
-    if (h->precision == 64)
-        h->d.runStage(stage, time_arg, adaptive != 0);
-    else
-        h->f.runStage(stage, float(time_arg), adaptive != 0);
-    return SF_OK;
+    return static_cast<sfo::Handle*>(hv)->visit([&](auto& sim) {
+        using T = typename std::decay<decltype(sim.maxAccLen)>::type;
+        sim.runStage(stage, T(time_arg), adaptive != 0);
+        return int(SF_OK);
+    });
 }
 
 // n substeps; adaptive != 0: each is UpdateSystem(time_arg), else dt = time_arg.
 int sfo_substeps(void* hv, double time_arg, int adaptive, int64_t n) {
-    auto* h = static_cast<sfo::Handle*>(hv);
-    for (int64_t k = 0; k < n; ++k) {
-        if (h->precision == 64)
-            h->d.substep(time_arg, adaptive != 0);
-        else
-            h->f.substep(float(time_arg), adaptive != 0);
-    }
-    return SF_OK;
+    return static_cast<sfo::Handle*>(hv)->visit([&](auto& sim) {
+        using T = typename std::decay<decltype(sim.maxAccLen)>::type;
+        for (int64_t k = 0; k < n; ++k) sim.substep(T(time_arg), adaptive != 0);
+        return int(SF_OK);
+    });
 }
 
 // The adaptive frame loop of seepage_flows/src/seepageflow/main.cpp:235-247.
 int sfo_frame_adaptive(void* hv, double render_interval, int64_t* n_calls) {
-    auto* h = static_cast<sfo::Handle*>(hv);
     int64_t calls = 0;
-    if (h->precision == 64) {
-        double remaining = render_interval;
-        while (remaining > 1e-6f) {
-            h->d.substep(remaining, true);
-            remaining -= remaining / double(h->d.numSub);
+    static_cast<sfo::Handle*>(hv)->visit([&](auto& sim) {
+        using T = typename std::decay<decltype(sim.maxAccLen)>::type;
+        T remaining = T(render_interval);
+        while (remaining > T(1e-6f)) {
+            sim.substep(remaining, true);
+            remaining -= remaining / T(sim.numSub);
             ++calls;
         }
-    } else {
-        float remaining = float(render_interval);
-        while (remaining > 1e-6f) {
-            h->f.substep(remaining, true);
-            remaining -= remaining / float(h->f.numSub);
-            ++calls;
-        }
-    }
+        return 0;
+    });
     if (n_calls) *n_calls = calls;
     return SF_OK;
 }
 
 int64_t sfo_num_substeps(void* hv) {
-    auto* h = static_cast<sfo::Handle*>(hv);
-    return h->precision == 64 ? h->d.numSub : h->f.numSub;
+    return static_cast<sfo::Handle*>(hv)->visit([&](auto& sim) { return sim.numSub; });
 }
 
 double sfo_max_acc(void* hv) {
+    return static_cast<sfo::Handle*>(hv)->visit([&](auto& sim) { return double(sim.maxAccLen); });
+}
+
+// Forward-mode handles (precision 65): tangents of positions / velocities
+// (3 doubles per particle, current internal order; before the first sort
+// that is the creation order) and the parameter to differentiate by.
+int sfo_set_tangent(void* hv, int field, const double* src, int64_t count) {
     auto* h = static_cast<sfo::Handle*>(hv);
-    return h->precision == 64 ? h->d.maxAccLen : double(h->f.maxAccLen);
+    if (h->precision != 65) return SF_ERR_INVALID;
+    return sfo::tangentField(h->j, field, nullptr, src, count);
+}
+
+int sfo_get_tangent(void* hv, int field, double* dst, int64_t count) {
+    auto* h = static_cast<sfo::Handle*>(hv);
+    if (h->precision != 65) return SF_ERR_INVALID;
+    return sfo::tangentField(h->j, field, dst, nullptr, count);
+}
+
+// which: 0 none, 1 tan friction angle, 2 capillary scale, 3 permeability scale.
+// The permeability tangent also seeds the per-particle cd of sand (MULTI scenes).
+int sfo_seed_param(void* hv, int which) {
+    auto* h = static_cast<sfo::Handle*>(hv);
+    if (h->precision != 65 || which < 0 || which > 3) return SF_ERR_INVALID;
+    h->j.seedParam = which;
+    for (int64_t i = 0; i < h->j.n; ++i) h->j.cda0asat[i].x.d = (which == 3 && h->j.label[i] == 1) ? h->j.cda0asat[i].x.v : 0.0;
+    return SF_OK;
 }
 
 // Largest distance at which a pair term can be non-zero for these params.

@@ -397,7 +397,7 @@ def capillary_rupture(r: float) -> float:
 
 def adjoint_probe(seed: int = 11, sand_counts=(5, 3, 5), water_counts=(5, 6, 8), gap: float = 0.012,
                   sand_velocity=(0.05, 0.0, 0.03), water_pitch: float = 0.019, water_speed: float = 0.01,
-                  margin: float = 5e-4) -> Scene:
+                  margin: float = 5e-4, sand_overlap: float = 0.0, sand_speed: float = 0.0) -> Scene:
     """A small scene whose short-horizon trajectory stays away from the
     model's value discontinuities, for gradient checks against finite
     differences: sand at pitch 2r + s_rupture / 2 (every lattice pair inside
@@ -407,7 +407,10 @@ def adjoint_probe(seed: int = 11, sand_counts=(5, 3, 5), water_counts=(5, 6, 8),
     given gap, moving at random velocities up to water_speed (so no pair
     sits on the viscosity switch dv . d = 0), no sand-water pair within margin
     of h / 2 or h (the ends of the adhesion spline) and no sand whose nearest
-    water lies within margin of h (voidage onset)."""
+    water lies within margin of h (voidage onset). With sand_overlap > 0 the
+    sand pitch is 2r - sand_overlap instead (every lattice pair in DEM
+    contact, no liquid bridges) and sand_speed adds random sand velocities
+    (sliding contacts at the friction cap)."""
     r = 0.01
     params = reference_params(sph_radius=r, dem_radius=r)
     h = params.sph_kernel_radius
@@ -416,11 +419,12 @@ def adjoint_probe(seed: int = 11, sand_counts=(5, 3, 5), water_counts=(5, 6, 8),
     sparams = solver_params()
     rng = np.random.default_rng(seed)
     srupt = capillary_rupture(r)
-    ps = 2.0 * r + 0.5 * srupt
+    ps = 2.0 * r + 0.5 * srupt if sand_overlap <= 0.0 else 2.0 * r - sand_overlap
     sx, sy, sz = sand_counts
     idx = np.stack(np.meshgrid(*[np.arange(c) for c in sand_counts], indexing="ij"), -1).reshape(-1, 3)
     sand = np.array([0.20, 0.0199, 0.5 * box[2] - 0.5 * (sz - 1) * ps]) + idx * ps
-    sand = sand + rng.uniform(-0.1 * srupt, 0.1 * srupt, size=sand.shape) * np.array([1.0, 0.2, 1.0])
+    jit = 0.1 * srupt if sand_overlap <= 0.0 else 0.05 * sand_overlap
+    sand = sand + rng.uniform(-jit, jit, size=sand.shape) * np.array([1.0, 0.2, 1.0])
     wx, wy, wz = water_counts
     widx = np.stack(np.meshgrid(*[np.arange(c) for c in water_counts], indexing="ij"), -1).reshape(-1, 3)
     wp = water_pitch
@@ -440,6 +444,8 @@ def adjoint_probe(seed: int = 11, sand_counts=(5, 3, 5), water_counts=(5, 6, 8),
     sc = _assemble("adjoint_probe", params, bparams, sparams, sand.astype(np.float32), water.astype(np.float32),
                    r, r, meta={"seed": seed, "sand_pitch": ps, "gap": gap})
     sc.vel[: sand.shape[0]] = np.asarray(sand_velocity, dtype=np.float32)
+    if sand_speed > 0.0:
+        sc.vel[: sand.shape[0]] += rng.uniform(-sand_speed, sand_speed, size=(sand.shape[0], 3)).astype(np.float32)
     sc.vel[sand.shape[0]:] = wvel.astype(np.float32)
     return sc
 

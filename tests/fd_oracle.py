@@ -29,6 +29,19 @@ def probe_scene(seed, damping):
     return sc
 
 
+# (seed, substeps, sand overlap, random sand speed) of the DEM-contact probes:
+# every sand lattice pair overlapping (no liquid bridges), sliding contacts,
+# no damping. Their loss has friction-cap kinks, so central differences
+# converge only at the fine step; the forward-mode oracle is their reference.
+CONTACT_CASES = [(21, 8, 4e-4, 0.02), (22, 8, 6e-4, 0.03)]
+
+
+def contact_scene(seed, overlap, speed):
+    sc = scenes.adjoint_probe(seed=seed, sand_overlap=overlap, sand_speed=speed, sand_velocity=(0.0, 0.0, 0.0))
+    sc.params.dem_damping = 0.0
+    return sc
+
+
 def probe_target(scene):
     return scene.pos.astype(np.float64) + TARGET_SHIFT
 
@@ -103,3 +116,24 @@ def checked_fd(fn, steps, consistency):
     rel = abs(a - b) / max(abs(b), 1e-300)
     assert rel <= consistency, f"finite differences not converged: {a:.9e} vs {b:.9e} (rel {rel:.2e})"
     return b
+
+
+def jvp(oracle_mod, scene, dt, n_sub, target, which, u=None) -> float:
+    """Exact pathwise directional derivative of the loss from the FP64
+    forward-mode oracle: along u for which = "pos" / "vel", or by the
+    parameter which = "tan" / "cap" / "perm"."""
+    o = oracle_mod.Oracle(scene, precision=65)
+    if which in ("pos", "vel"):
+        o.set_tangent(which, u)   # creation order before the first sort
+    else:
+        o.seed_param(which)
+    o.substeps(dt, False, n_sub)
+    p = o.field("pos")
+    t = o.tangent("pos")
+    ids = o.field("id").astype(np.int64)
+    x = np.empty_like(p)
+    dx = np.empty_like(t)
+    x[ids] = p
+    dx[ids] = t
+    sand = scene.label == SF_LABEL_SAND
+    return float(np.mean(np.sum(2.0 * (x[sand] - target[sand]) * dx[sand], axis=1)))
