@@ -238,6 +238,38 @@ def adjoint_comparison(stream, n_substeps=200, checkpoint_every=20):
     return out
 
 
+def adjoint_workload(args):
+    """--adjoint-substeps K: the gradient run on the bench workload alone (K
+    substeps, every substep stored), forward and reverse device time per
+    substep against the graph-replayed forward; used for the ncu launch list
+    of the adjoint kernels."""
+    import torch
+
+    from sph_seepage_flows_gb300 import capi
+    sc = make_scene(args.workload)
+    dt = reference_dt(sc)
+    k = args.adjoint_substeps
+    sim = capi.Simulation(sc)
+    sim.autotune(dt)
+    target = sc.pos.astype(np.float32) + np.float32(1e-3)
+    sim.adjoint(dt, k, target, want_state_grads=False)  # allocates the stored substeps
+    r = sim.adjoint(dt, k, target, want_state_grads=False)
+    stream = torch.cuda.Stream()
+    fwd = capi.Simulation(sc, stream=stream.cuda_stream)
+    fwd.substeps_fixed(dt, 2)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fwd.substeps_fixed(dt, k)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    print(json.dumps({"adjoint_workload": args.workload, "particles": sc.n, "substeps": k,
+                      "forward_ms_per_substep": ms / k, "store_forward_ms_per_substep": r["ms_forward"] / k,
+                      "reverse_ms_per_substep": r["ms_reverse"] / k,
+                      "gradient_run_vs_forward": (r["ms_forward"] + r["ms_reverse"]) / ms}), flush=True)
+
+
 def calibration_timing(stream, iterations=2, n_substeps=500, checkpoint_every=25):
     """Per-iteration time of the batched calibration workload (32 scenes of
     10k-50k particles, 500 substeps, checkpoints every 25): `iterations`
@@ -436,7 +468,12 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-calibration", action="store_true")
+    ap.add_argument("--adjoint-substeps", type=int, default=0,
+                    help="only time the gradient run of the workload over this many substeps")
     args = ap.parse_args()
+    if args.adjoint_substeps > 0:
+        adjoint_workload(args)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

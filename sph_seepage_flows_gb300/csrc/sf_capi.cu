@@ -206,7 +206,8 @@ struct sf_handle {
     size_t stageBytes = 0;
     bool sorted = false;
     int64_t launches = 0;
-    GraphCache graph[2];
+    GraphCache graph[2];   // two-substep graphs, by starting buffer set
+    GraphCache graph1[2];  // one-substep graphs, by starting buffer set
     int nbrCap = kMinNbr;                 // particle neighbour list capacity (per slot)
     int block[kTunedPasses] = {kSlotAlign, kSlotAlign, kSlotAlign, kSlotAlign, kSlotAlign, kSlotAlign};
     unsigned int* dProbe = nullptr;       // neighbour-count probe word
@@ -278,6 +279,12 @@ struct sf_handle {
     }
     // Drop the captured substep graphs (after a change of buffers or launch shapes).
     void dropGraphs() {
+        for (auto& g : graph1) {
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+            g.dt = 0.f;
+            g.nodes = 0;
+        }
         for (auto& g : graph) {
             if (g.exec) cudaGraphExecDestroy(g.exec);
             g.exec = nullptr;
@@ -287,6 +294,8 @@ struct sf_handle {
     }
     ~sf_handle() {
         for (auto& g : graph)
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+        for (auto& g : graph1)
             if (g.exec) cudaGraphExecDestroy(g.exec);
         devFree(dProbe);
         for (int k = 0; k < 2; ++k) {
@@ -748,47 +757,54 @@ sf_status sf_frame_adaptive(sf_handle* h, float render_interval, int64_t* n_call
     return SF_OK;
 }
 
+// The captured graph of `nsub` fixed-dt substeps starting from buffer set
+// h->cur (captured on first use and whenever dt changes).
+static sf_status ensureGraph(sf_handle* h, GraphCache& g, int nsub, float dt) {
+    if (g.exec && g.dt == dt) return SF_OK;
+    if (g.exec) {
+        cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+    }
+    const int curBefore = h->cur;
+    const int64_t launchesBefore = h->launches;
+    cudaGraph_t graph = nullptr;
+    sf_status st = h->cuda(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    if (st) return st;
+    for (int k = 0; k < nsub && st == SF_OK; ++k) st = runSubstep(h, dt, 0);
+    cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+    h->cur = curBefore;
+    g.nodes = int(h->launches - launchesBefore);
+    h->launches = launchesBefore;
+    if (st != SF_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return st;
+    }
+    if (h->cuda(ce, "end capture")) return SF_ERR_CUDA;
+    st = h->cuda(cudaGraphInstantiate(&g.exec, graph, 0), "graph instantiate");
+    cudaGraphDestroy(graph);
+    if (st) return st;
+    g.dt = dt;
+    return SF_OK;
+}
+
 sf_status sf_substeps_fixed(sf_handle* h, float dt, int64_t n) {
     if (!h || n < 0) return SF_ERR_INVALID;
-    int64_t k = 0;
-    // odd remainder (or a single step) without a graph
-    if (n % 2 == 1) {
-        sf_status st = runSubstep(h, dt, 0);
-        if (st != SF_OK) return st;
-        k = 1;
+    if (n == 0) return SF_OK;
+    sf_status st = SF_OK;
+    if (n % 2 == 1) {  // the odd substep from a one-substep graph of this buffer set
+        GraphCache& g1 = h->graph1[h->cur];
+        if ((st = ensureGraph(h, g1, 1, dt))) return st;
+        if (h->cuda(cudaGraphLaunch(g1.exec, h->stream), "graph launch")) return SF_ERR_CUDA;
+        h->launches += g1.nodes;
+        h->cur = 1 - h->cur;
     }
-    if (n - k <= 0) return SF_OK;
-    GraphCache& g = h->graph[h->cur];
-    if (!g.exec || g.dt != dt) {
-        if (g.exec) {
-            cudaGraphExecDestroy(g.exec);
-            g.exec = nullptr;
+    if (n >= 2) {
+        GraphCache& g = h->graph[h->cur];
+        if ((st = ensureGraph(h, g, 2, dt))) return st;
+        for (int64_t k = n % 2; k + 2 <= n; k += 2) {
+            if (h->cuda(cudaGraphLaunch(g.exec, h->stream), "graph launch")) return SF_ERR_CUDA;
+            h->launches += g.nodes;
         }
-        const int curBefore = h->cur;
-        const int64_t launchesBefore = h->launches;
-        cudaGraph_t graph = nullptr;
-        sf_status st = h->cuda(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-        if (st) return st;
-        sf_status s1 = runSubstep(h, dt, 0);
-        sf_status s2 = s1 == SF_OK ? runSubstep(h, dt, 0) : s1;
-        cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
-        h->cur = curBefore;
-        g.nodes = int(h->launches - launchesBefore);
-        h->launches = launchesBefore;
-        if (s2 != SF_OK) {
-            if (graph) cudaGraphDestroy(graph);
-            return s2;
-        }
-        if (h->cuda(ce, "end capture")) return SF_ERR_CUDA;
-        st = h->cuda(cudaGraphInstantiate(&g.exec, graph, 0), "graph instantiate");
-        cudaGraphDestroy(graph);
-        if (st) return st;
-        g.dt = dt;
-    }
-    for (; k + 2 <= n; k += 2) {
-        sf_status st = h->cuda(cudaGraphLaunch(g.exec, h->stream), "graph launch");
-        if (st) return st;
-        h->launches += g.nodes;
     }
     h->sorted = true;
     return SF_OK;
@@ -902,6 +918,17 @@ int fieldWidth(int field) {
     }
 }
 
+// Device address of page-locked (pinned) host memory, which kernels can
+// read and write directly over the host link; nullptr for other memory.
+void* mappedHostPointer(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 sf_status ensureStage(sf_handle* h, size_t bytes) {
     if (h->stageBytes >= bytes) return SF_OK;
     if (h->stage) cudaFree(h->stage);
@@ -944,9 +971,16 @@ sf_status sf_get_field(sf_handle* h, int32_t scene, int32_t field, int32_t order
     const size_t bytes = size_t(n) * size_t(w) * 4;
     if (n == 0) return SF_OK;
     void* target = dst;
+    // pinned host memory in sorted order is written by the gather kernel
+    // directly (coalesced); anything else goes through the device stage
+    void* mapped = (!dst_on_device && order == SF_ORDER_SORTED) ? mappedHostPointer(dst) : nullptr;
     if (!dst_on_device) {
-        if (ensureStage(h, bytes)) return SF_ERR_CUDA;
-        target = h->stage;
+        if (mapped) {
+            target = mapped;
+        } else {
+            if (ensureStage(h, bytes)) return SF_ERR_CUDA;
+            target = h->stage;
+        }
     }
     const int blocks = int((n + 255) / 256);
     if (bfield) {
@@ -960,7 +994,8 @@ sf_status sf_get_field(sf_handle* h, int32_t scene, int32_t field, int32_t order
     }
     if (h->cuda(cudaGetLastError(), "get_field launch")) return SF_ERR_CUDA;
     if (!dst_on_device) {
-        if (h->cuda(cudaMemcpyAsync(dst, h->stage, bytes, cudaMemcpyDeviceToHost, h->stream), "get_field D2H"))
+        if (!mapped &&
+            h->cuda(cudaMemcpyAsync(dst, h->stage, bytes, cudaMemcpyDeviceToHost, h->stream), "get_field D2H"))
             return SF_ERR_CUDA;
         return h->cuda(cudaStreamSynchronize(h->stream), "get_field sync");
     }
@@ -981,11 +1016,17 @@ sf_status sf_set_field(sf_handle* h, int32_t scene, int32_t field, int32_t order
     if (n == 0) return SF_OK;
     const size_t bytes = size_t(n) * size_t(w) * 4;
     const void* from = src;
+    // pinned host memory in sorted order is read by the scatter kernel directly
+    void* mapped = (!src_on_device && order == SF_ORDER_SORTED) ? mappedHostPointer(src) : nullptr;
     if (!src_on_device) {
-        if (ensureStage(h, bytes)) return SF_ERR_CUDA;
-        if (h->cuda(cudaMemcpyAsync(h->stage, src, bytes, cudaMemcpyHostToDevice, h->stream), "set_field H2D"))
-            return SF_ERR_CUDA;
-        from = h->stage;
+        if (mapped) {
+            from = mapped;
+        } else {
+            if (ensureStage(h, bytes)) return SF_ERR_CUDA;
+            if (h->cuda(cudaMemcpyAsync(h->stage, src, bytes, cudaMemcpyHostToDevice, h->stream), "set_field H2D"))
+                return SF_ERR_CUDA;
+            from = h->stage;
+        }
     }
     const int c = h->cur;
     kSetField<<<int((n + 255) / 256), 256, 0, h->stream>>>(field, int(n), S.slot_off, order, h->pos[c], h->vel[c],
