@@ -154,7 +154,10 @@ enum {
     SF_STAGE_SORT = 0,              /* hash, stable radix sort by cell, reorder, cell tables */
     SF_STAGE_DENSITY = 1,           /* density + Tait/linear pressure */
     SF_STAGE_AVGFLOW = 2,           /* average flow, fluid voidage, saturation */
-    SF_STAGE_VOIDAGE_ADHESION = 3,  /* sand voidage, water adhesion, wet-sand colour */
+    SF_STAGE_VOIDAGE_ADHESION = 3,  /* sand voidage, water adhesion, wet-sand colour; also each
+                                       water particle's rho / voidage and pressure term, which the
+                                       momentum stages read (set density, pressure or voidage
+                                       before this stage, not after it) */
     SF_STAGE_SAND_MOMENTUM = 4,     /* acc = g + sand forces; average drag */
     SF_STAGE_WATER_MOMENTUM = 5,    /* acc = g + water forces; max |acc| */
     SF_STAGE_INTEGRATE = 6,         /* CFL dt, damping, Euler, water clamp, next keys */

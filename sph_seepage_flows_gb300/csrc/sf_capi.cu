@@ -191,6 +191,7 @@ struct sf_handle {
     int cur = 0;
     // per-substep arrays
     float4 *aux = nullptr, *flow = nullptr, *adh = nullptr, *avgadh = nullptr, *drag = nullptr, *acc = nullptr;
+    float2* dp = nullptr;
     unsigned int *keys = nullptr, *cs = nullptr, *bcs = nullptr;
     unsigned int* nbrCnt = nullptr;
     int* bnbrCnt = nullptr;
@@ -275,6 +276,7 @@ struct sf_handle {
         b.col4 = col[cur];
         b.mat4 = mat[cur];
         b.bpos4 = bpos;
+        b.dp = dp;
         return b;
     }
     // Drop the captured substep graphs (after a change of buffers or launch shapes).
@@ -312,6 +314,7 @@ struct sf_handle {
         devFree(avgadh);
         devFree(drag);
         devFree(acc);
+        devFree(dp);
         devFree(keys);
         devFree(nbrCnt);
         devFree(bnbrCnt);
@@ -569,6 +572,7 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
     SF_ALLOC(h->avgadh, F4);
     SF_ALLOC(h->drag, F4);
     SF_ALLOC(h->acc, F4);
+    SF_ALLOC(h->dp, sizeof(float2) * M);
     SF_ALLOC(h->keys, sizeof(unsigned) * M);
     SF_ALLOC(h->nbrCnt, sizeof(unsigned) * M);
     SF_ALLOC(h->bnbrCnt, sizeof(int) * M);

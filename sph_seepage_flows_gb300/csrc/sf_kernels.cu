@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(kSlotAlign) kAvgFlow(const SceneDev* __restric
 __global__ void __launch_bounds__(kSlotAlign) kVoidageAdhesion(
     const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene, NbrLists L,
     const float4* __restrict__ pos4, const float4* __restrict__ vel4, float4* __restrict__ aux4,
-    float4* __restrict__ adh4, float4* __restrict__ avgadh4, float4* __restrict__ col4) {
+    float4* __restrict__ adh4, float4* __restrict__ avgadh4, float4* __restrict__ col4, float2* __restrict__ dp) {
     SF_SLOT_PROLOGUE
     const float4 pi4 = pos4[slot];
     if (pi4.w == 0.f) return;
@@ -318,6 +318,11 @@ __global__ void __launch_bounds__(kSlotAlign) kVoidageAdhesion(
         adh4[slot] = make_float4(ad.x, ad.y, ad.z, 0.f);
         const float3 avg = v_s != 0.f ? ad / v_s : mk3(0.f, 0.f, 0.f);
         avgadh4[slot] = make_float4(avg.x, avg.y, avg.z, 0.f);
+        // the effective density and pressure term, with the operations every
+        // momentum pair term of this particle uses
+        const float4 ai = aux4[slot];
+        const float D = vel4[slot].w / fmaxf(kEps, ai.w);
+        dp[slot] = make_float2(D, ai.x / fmaxf(kEps, D * D));
     }
 }
 
@@ -331,7 +336,8 @@ __global__ void __launch_bounds__(kSlotAlign) kSandMomentum(
     const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene, NbrLists L,
     const float4* __restrict__ pos4, const float4* __restrict__ vel4, const float4* __restrict__ aux4,
     const float4* __restrict__ flow4, const float4* __restrict__ avgadh4, const float4* __restrict__ mat4,
-    const float4* __restrict__ bpos4, float4* __restrict__ drag4, float4* __restrict__ acc4) {
+    const float4* __restrict__ bpos4, const float2* __restrict__ dp, float4* __restrict__ drag4,
+    float4* __restrict__ acc4) {
     SF_SLOT_PROLOGUE
     const float4 pi4 = pos4[slot];
     if (!(pi4.w < 0.f)) {
@@ -372,7 +378,7 @@ __global__ void __launch_bounds__(kSlotAlign) kSandMomentum(
         const float4 aj = aux4[j];
         const float wij = poly6(S, len3(dij));
         if (aj.w > 0.f && aj.w <= 1.f) {
-            const float dj = vel4[j].w / fmaxf(kEps, aj.w);
+            const float dj = dp[j].x;
             v_w += pj.w / dj * wij;
             f += -mi * pj.w * aj.x / fmaxf(kEps, di * dj) * spikyGrad(S, dij);
         }
@@ -421,7 +427,7 @@ __global__ void __launch_bounds__(kSlotAlign) kWaterMomentum(
     const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene, SceneState* __restrict__ state,
     NbrLists L, const float4* __restrict__ pos4, const float4* __restrict__ vel4, const float4* __restrict__ aux4,
     const float4* __restrict__ drag4, const float4* __restrict__ adh4, const float4* __restrict__ bpos4,
-    float4* __restrict__ acc4, unsigned int* errWord) {
+    const float2* __restrict__ dp, float4* __restrict__ acc4, unsigned int* errWord) {
     SF_SLOT_PROLOGUE
     const float4 pi4 = pos4[slot];
     float alen = 0.f;
@@ -429,20 +435,20 @@ __global__ void __launch_bounds__(kSlotAlign) kWaterMomentum(
         const float3 pi = xyz(pi4);
         const float4 vi4 = vel4[slot];
         const float3 vi = xyz(vi4);
-        const float4 ai4 = aux4[slot];
-        const float di = vi4.w / fmaxf(kEps, ai4.w);
-        const float pri = ai4.x;
-        const float pterm_i = pri / fmaxf(kEps, di * di);
+        const float2 dpi = dp[slot];
+        const float di = dpi.x;
+        const float pri = aux4[slot].x;
+        const float pterm_i = dpi.y;
         float3 a = mk3(0.f, 0.f, 0.f);
         forWaterNeighbors(S, L, slot, pi, pos4, [&](int j) {
             if (j == slot) return;
             const float4 pj = pos4[j];
             const float3 dij = pi - xyz(pj);
-            const float4 aj = aux4[j];
+            const float2 dpj = dp[j];
             const float4 vj4 = vel4[j];
-            const float dj = vj4.w / fmaxf(kEps, aj.w);
+            const float dj = dpj.x;
             const float3 nab = spikyGrad(S, dij);
-            a += -pj.w * (pterm_i + aj.x / fmaxf(kEps, dj * dj)) * nab;
+            a += -pj.w * (pterm_i + dpj.y) * nab;
             const float dd = dot3(vi - xyz(vj4), dij);
             if (dd < 0.f) {
                 const float pij = -S.nu / (di + dj) * (dd / (dot3(dij, dij) + kEps));
@@ -631,19 +637,19 @@ void launchAvgFlow(const LaunchCtx& c, const PassBuffers& b) {
 
 void launchVoidageAdhesion(const LaunchCtx& c, const PassBuffers& b) {
     kVoidageAdhesion<<<grid(c, kPassVoidage), c.block[kPassVoidage], 0, c.stream>>>(c.scenes, c.blockScene, b.lists, b.pos4, b.vel4,
-                                                                b.aux4, b.adh4, b.avgadh4, b.col4);
+                                                                b.aux4, b.adh4, b.avgadh4, b.col4, b.dp);
 }
 
 void launchSandMomentum(const LaunchCtx& c, const PassBuffers& b) {
     kSandMomentum<<<grid(c, kPassSand), c.block[kPassSand], 0, c.stream>>>(c.scenes, c.blockScene, b.lists, b.pos4, b.vel4,
-                                                             b.aux4, b.flow4, b.avgadh4, b.mat4, b.bpos4, b.drag4,
-                                                             b.acc4);
+                                                             b.aux4, b.flow4, b.avgadh4, b.mat4, b.bpos4, b.dp,
+                                                             b.drag4, b.acc4);
 }
 
 void launchWaterMomentum(const LaunchCtx& c, const PassBuffers& b) {
     kWaterMomentum<<<grid(c, kPassWater), c.block[kPassWater], 0, c.stream>>>(c.scenes, c.blockScene, c.state, b.lists, b.pos4,
-                                                              b.vel4, b.aux4, b.drag4, b.adh4, b.bpos4, b.acc4,
-                                                              c.errWord);
+                                                              b.vel4, b.aux4, b.drag4, b.adh4, b.bpos4, b.dp,
+                                                              b.acc4, c.errWord);
 }
 
 void launchIntegrate(const LaunchCtx& c, const PassBuffers& b, float timeArg, int adaptive) {

@@ -78,6 +78,10 @@ struct PassBuffers {
     float4* col4;
     float4* mat4;
     const float4* bpos4;
+    // water: (D, P) = (rho / max(eps, voidage), p / max(eps, D^2)), the
+    // effective density and pressure term every momentum pair term of the
+    // particle uses (written by the voidage / adhesion pass)
+    float2* dp;
 };
 
 void launchKeys(const LaunchCtx& c, const float4* pos4, unsigned int* keys);
