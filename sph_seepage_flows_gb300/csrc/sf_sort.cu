@@ -18,7 +18,7 @@
 namespace sfg {
 
 constexpr int kSortThreads = 256;
-constexpr int kSortItems = 16;
+constexpr int kSortItems = 8;
 constexpr int kTile = kSortThreads * kSortItems;
 
 int sortTiles(int n) { return (n + kTile - 1) / kTile; }
