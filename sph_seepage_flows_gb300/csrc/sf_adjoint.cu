@@ -370,8 +370,9 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjWater(const SceneDev* __restri
         const float mk = pk4.w;
         const float3 ak = xyz(A.acc[slot]);
         A.adh[slot] = f4(ak / -mk);
-        const float Dk = rhoK / fmaxf(kEps, epsK);
-        const float Pk = pK / fmaxf(kEps, Dk * Dk);
+        const float2 dpk = b.dp[slot];
+        const float Dk = dpk.x;
+        const float Pk = dpk.y;
         float Pbar = 0.f, Dbar = 0.f, pbar = 0.f;
         LabelCursor<false> wc(S, L, slot, xk, b.pos4);
         for (int j; wc.next(j);) {
@@ -381,9 +382,9 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjWater(const SceneDev* __restri
             const SpikyD sp = spikyD(S, d);
             if (sp.phi == 0.f && sp.psi == 0.f) continue;
             const float4 vj4 = b.vel4[j];
-            const float4 aj4 = b.aux4[j];
-            const float Dj = vj4.w / fmaxf(kEps, aj4.w);
-            const float Pj = aj4.x / fmaxf(kEps, Dj * Dj);
+            const float2 dpj = b.dp[j];
+            const float Dj = dpj.x;
+            const float Pj = dpj.y;
             const float3 c = pj4.w * ak - mk * xyz(A.acc[j]);
             const float cg = dot3(c, sp.g);
             float coef = -(Pk + Pj);
@@ -455,7 +456,7 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjWater(const SceneDev* __restri
             const float4 pi4 = b.pos4[i];
             const float3 d = xyz(pi4) - xk;
             const SpikyD sp = spikyD(S, d);
-            const float Di = b.vel4[i].w / fmaxf(kEps, b.aux4[i].w);
+            const float Di = b.dp[i].x;
             const float3 ai = xyz(A.acc[i]);
             const float alpha = -mk * b.aux4[i].x / fmaxf(kEps, Di * rhoK);
             gx -= alpha * spikyVjp(sp, d, ai) + (-dot3(ai, dragK) / Di) * poly6Grad(S, d);
@@ -592,7 +593,7 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjSandPairs(const SceneDev* __re
                 gx += (volK * dot3(fb, xyz(b.avgadh4[j]))) * gW;
                 const float ej = b.aux4[j].w;
                 if (ej > 0.f && ej <= 1.f) {
-                    const float Dj = b.vel4[j].w / fmaxf(kEps, ej);
+                    const float Dj = b.dp[j].x;
                     const float sigma = -mk * pj4.w * b.aux4[j].x / fmaxf(kEps, rhoK * Dj);
                     gx += sigma * spikyVjp(spikyD(S, d), d, fb) + (vwb * pj4.w / Dj) * gW;
                 }

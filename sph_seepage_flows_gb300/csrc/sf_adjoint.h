@@ -35,6 +35,7 @@ struct AdjSlab {
     unsigned int* cnbr;
     unsigned int* cs;
     float4 *aux, *flow, *drag, *acc, *adh, *avgadh, *pos, *vel, *mat;
+    float2* dp;
     int* pid;
 };
 // Copies the fields the integrator overwrites (pos, vel, acc, adhesion,

@@ -1247,7 +1247,7 @@ sf_status snapCopy(sf_handle* h, char* snap, bool save) {
 size_t slabStride(const sf_handle* h) {
     const size_t M = size_t(h->totalSlots);
     const size_t b = M * (sizeof(unsigned) * (1 + size_t(h->nbrCap) + kMaxContact) + sizeof(int) * 2 + sizeof(unsigned) * kMaxBNbr +
-                          9 * sizeof(float4) + sizeof(int)) +
+                          9 * sizeof(float4) + sizeof(float2) + sizeof(int)) +
                      sizeof(unsigned) * (size_t(h->totalCells) + 1);
     return (b + 255) / 256 * 256;
 }
@@ -1270,6 +1270,7 @@ AdjSlab slabAt(const sf_handle* h, char* base) {
     s.adh = reinterpret_cast<float4*>(take(sizeof(float4) * M));
     s.avgadh = reinterpret_cast<float4*>(take(sizeof(float4) * M));
     s.mat = reinterpret_cast<float4*>(take(sizeof(float4) * M));
+    s.dp = reinterpret_cast<float2*>(take(sizeof(float2) * M));
     s.nbr = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * M * size_t(h->nbrCap)));
     s.bnbr = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * M * kMaxBNbr));
     s.cnbr = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * M * kMaxContact));
@@ -1301,6 +1302,7 @@ PassBuffers slabBuffers(const sf_handle* h, const AdjSlab& s) {
     b.adh4 = s.adh;
     b.avgadh4 = s.avgadh;
     b.mat4 = s.mat;
+    b.dp = s.dp;
     b.col4 = nullptr;
     return b;
 }
@@ -1313,6 +1315,8 @@ sf_status runSubstepStore(sf_handle* h, float dt, const AdjSlab& s) {
     unsigned *cnt = h->nbrCnt, *nbr = h->nbr, *bnbr = h->bnbr, *cnbr = h->cnbr, *cs = h->cs;
     int *bcnt = h->bnbrCnt, *ccnt = h->cnbrCnt;
     float4 *aux = h->aux, *flow = h->flow, *drag = h->drag;
+    float2* dp = h->dp;
+    h->dp = s.dp;
     h->nbrCnt = s.cnt;
     h->nbr = s.nbr;
     h->bnbr = s.bnbr;
@@ -1339,6 +1343,7 @@ sf_status runSubstepStore(sf_handle* h, float dt, const AdjSlab& s) {
     h->aux = aux;
     h->flow = flow;
     h->drag = drag;
+    h->dp = dp;
     if (st != SF_OK) return st;
     return runStage(h, SF_STAGE_INTEGRATE, dt, 0);
 }
