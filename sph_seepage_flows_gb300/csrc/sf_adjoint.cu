@@ -496,9 +496,9 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjSandSelf(const SceneDev* __res
                                        cd, dseed<8>(1.f, 7));
         float3 dfb = fb;
         float vwb = 0.f;
-        if (vw != 0.f) {
+        if (vw != 0.f) {  // avg drag = df / v_w: d/dv_w = -avg drag / v_w
             dfb = dfb + dragB / vw;
-            vwb = -dot3(dragB, mk3(df.x.v, df.y.v, df.z.v)) / (vw * vw);
+            vwb = -dot3(dragB, mk3(df.x.v, df.y.v, df.z.v) / vw) / vw;
         }
         A.s[slot].z += vjp(dfb, df, 0);
         A.flow[slot] = f4(vjp3(dfb, df, 1));
@@ -665,8 +665,9 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjVoidSelf(const SceneDev* __res
             num += b.aux4[j].y * vj * wij;
             den += vj * wij;
         }
+        // quotient rule without squaring den (a small den would underflow)
         const float eb = A.s[slot].z;
-        A.r[slot] = den != 0.f ? make_float4(eb / den, -eb * num / (den * den), 0.f, 0.f)
+        A.r[slot] = den != 0.f ? make_float4(eb / den, -(eb / den) * (num / den), 0.f, 0.f)
                                : make_float4(0.f, 0.f, 0.f, 0.f);
     } else {
         float vs = 0.f;
@@ -678,9 +679,9 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjVoidSelf(const SceneDev* __res
         const float3 avgB = xyz(A.avgadh[slot]);
         float3 tot = xyz(A.adh[slot]);
         float vsb = 0.f;
-        if (vs != 0.f) {
+        if (vs != 0.f) {  // avg = F / v_s: d/dv_s = -avg / v_s
             tot = tot + avgB / vs;
-            vsb = -dot3(avgB, xyz(b.adh4[slot])) / (vs * vs);
+            vsb = -dot3(avgB, xyz(b.avgadh4[slot])) / vs;
         }
         A.r[slot] = f4(tot, vsb);
     }

@@ -162,3 +162,21 @@ def test_autograd_function(cuda_lib):
     r = sim.adjoint(DT, 8, probe_target(sc))
     assert np.allclose(x0.grad.numpy(), 3.0 * r["grad_pos0"], rtol=1e-6, atol=0)
     assert np.allclose(v0.grad.numpy(), 3.0 * r["grad_vel0"], rtol=1e-6, atol=0)
+
+
+def test_long_horizon_gradients_stay_finite(cuda_lib):
+    """200 substeps of the 20k column, twice (the second run starts from a
+    re-set state whose particles are in another slot order): the cotangents
+    grow by orders of magnitude but no quotient-rule term may overflow to a
+    non-finite value."""
+    from sph_seepage_flows_gb300 import calibrate, scenes
+    from sph_seepage_flows_gb300.params import reference_dt
+    sc = scenes.adjoint_column()
+    dt = reference_dt(sc.params, sc.bparams, sc.sparams)[1]
+    target = calibrate.forward_targets([sc], [np.array([sc.params.dem_tan_friction_angle, 1.1, 1.1])], dt, 200)[0]
+    sim = sim_of(sc)
+    for _ in range(2):
+        r = sim.adjoint(dt, 200, target)
+        for key in ("loss", "grad_params", "grad_pos0", "grad_vel0"):
+            assert np.all(np.isfinite(r[key])), key
+        calibrate.reset_state(sim, 0, sc)
