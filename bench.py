@@ -60,8 +60,8 @@ BYTES_PER_SUBSTEP = sum(STAGE_BYTES.values())  # 753
 
 # DRAM bytes (read + write) per launch of each stage's main kernel on the 1M
 # workload, from the committed ncu capture (profiles/neighbor_passes_1M_ncu.md).
-NCU_TRAFFIC = {"density": 309.2e6, "avgflow": 116.8e6, "water_momentum": 128.8e6,
-               "sand_momentum": 54.6e6, "voidage_adhesion": 41.8e6}
+NCU_TRAFFIC = {"density": 285.1e6, "avgflow": 120.5e6, "water_momentum": 133.0e6,
+               "sand_momentum": 54.9e6, "voidage_adhesion": 60.7e6}
 
 
 def peaks():
@@ -253,7 +253,9 @@ def adjoint_workload(args):
     sim.autotune(dt)
     target = sc.pos.astype(np.float32) + np.float32(1e-3)
     sim.adjoint(dt, k, target, want_state_grads=False)  # allocates the stored substeps
+    torch.cuda.nvtx.range_push("timed")
     r = sim.adjoint(dt, k, target, want_state_grads=False)
+    torch.cuda.nvtx.range_pop()
     stream = torch.cuda.Stream()
     fwd = capi.Simulation(sc, stream=stream.cuda_stream)
     fwd.substeps_fixed(dt, 2)
@@ -347,9 +349,11 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize()
     l0 = sim.launches()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("timed")  # lets a profiler capture exactly the timed substeps
     e0.record(stream)
     sim.substeps_fixed(dt, steps)
     e1.record(stream)
+    torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     barrier()
     ms = e0.elapsed_time(e1)
