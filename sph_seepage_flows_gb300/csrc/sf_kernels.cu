@@ -104,11 +104,67 @@ __device__ __forceinline__ float exactDensity(const SceneDev& S, const NbrListsW
     return d;
 }
 
-// Conservative reach test for building the lists: evaluated with fused
-// multiply-adds (cheaper); any pair it admits or rejects differently from the
-// exact test lies within 1e-5 of the reach, where every term is exactly zero.
-__device__ __forceinline__ bool inReachFast(const SceneDev& S, float3 d) {
-    return __fmaf_rn(d.x, d.x, __fmaf_rn(d.y, d.y, __fmul_rn(d.z, d.z))) < S.reach2;
+// Conservative reach test for building the lists, as a sign: negative when
+// the pair is in reach. Evaluated with fused multiply-adds (cheaper); any
+// pair it admits or rejects differently from the exact test lies within 1e-5
+// of the reach, where every term is exactly zero.
+__device__ __forceinline__ float reachSign(const SceneDev& S, float3 d) {
+    return __fmaf_rn(d.x, d.x, __fmaf_rn(d.y, d.y, __fmaf_rn(d.z, d.z, -S.reach2)));
+}
+__device__ __forceinline__ bool inReachFast(const SceneDev& S, float3 d) { return reachSign(S, d) < 0.f; }
+
+// Water density from the lists: m_i W(0), then cell by cell of the stencil
+// the water neighbours of the cell and the boundary neighbours of the cell
+// (both lists are in stencil order, i.e. in increasing cell index, so the
+// walk merges them by the cell tables). Terms of listed pairs beyond the
+// exact reach are +0, which leaves every partial sum unchanged.
+__device__ __forceinline__ float listDensity(const SceneDev& S, const NbrListsW& L, int slot, int cW, int bc,
+                                             float3 pi, float mi, const float4* __restrict__ pos4,
+                                             const float4* __restrict__ bpos4) {
+    float d = mi * S.W0;
+    const long long M = L.M;
+    const unsigned* __restrict__ wp = L.nbr + slot + size_t(L.cap - 1) * M;
+    if (bc == 0) {
+        int k = 0;
+        for (; k + 4 <= cW; k += 4) {
+            const unsigned j0 = wp[-k * M], j1 = wp[-(k + 1) * M], j2 = wp[-(k + 2) * M], j3 = wp[-(k + 3) * M];
+            const float4 p0 = pos4[j0], p1 = pos4[j1], p2 = pos4[j2], p3 = pos4[j3];
+            d += p0.w * poly6(S, len3(pi - xyz(p0)));
+            d += p1.w * poly6(S, len3(pi - xyz(p1)));
+            d += p2.w * poly6(S, len3(pi - xyz(p2)));
+            d += p3.w * poly6(S, len3(pi - xyz(p3)));
+        }
+        for (; k < cW; ++k) {
+            const float4 pj = pos4[wp[-k * M]];
+            d += pj.w * poly6(S, len3(pi - xyz(pj)));
+        }
+        return d;
+    }
+    const unsigned* __restrict__ bp = L.bnbr + slot;
+    const int3 c = cellOf(S, pi);
+    const int z0 = max(c.z - 1, 0), z1 = min(c.z + 1, S.gz - 1) + 1;
+    int kw = 0, kb = 0;
+    for (int x = max(c.x - 1, 0); x <= min(c.x + 1, S.gx - 1); ++x)
+        for (int y = max(c.y - 1, 0); y <= min(c.y + 1, S.gy - 1); ++y) {
+            const int base = S.cell_off + (x * S.gy + y) * S.gz;
+            for (int z = z0; z < z1; ++z) {
+                const unsigned wEnd = L.cs[base + z + 1];
+                for (; kw < cW; ++kw) {
+                    const unsigned j = wp[-kw * M];
+                    if (j >= wEnd) break;
+                    const float4 pj = pos4[j];
+                    d += pj.w * poly6(S, len3(pi - xyz(pj)));
+                }
+                const unsigned bEnd = L.bcs[base + z + 1];
+                for (; kb < bc; ++kb) {
+                    const unsigned j = bp[kb * M];
+                    if (j >= bEnd) break;
+                    const float4 bj = bpos4[j];
+                    d += S.rho0 * fabsf(bj.w) * poly6(S, len3(pi - xyz(bj)));
+                }
+            }
+        }
+    return d;
 }
 
 // Builds the neighbour lists (sand / water / boundary, each in stencil
@@ -117,7 +173,9 @@ __device__ __forceinline__ bool inReachFast(const SceneDev& S, float3 d) {
 // ComputeSFPressure_CUDA (cuda_sph_sf_solver_gpu.cuh:482-508). The stencil is
 // walked as 9 contiguous ranges (the 3 z-cells of one (dx, dy) column are
 // adjacent in the sorted order), which visits the same particles in the same
-// order as the 27-cell loop with far fewer divergent loop exits.
+// order as the 27-cell loop with far fewer divergent loop exits. The walk
+// only appends list entries; the contact filter and the density sum then run
+// over the finished lists, where the lanes of a warp stay together.
 __global__ void __launch_bounds__(kSlotAlign) kDensity(const SceneDev* __restrict__ scenes,
                                                        const int* __restrict__ blockScene,
                                                        SceneState* __restrict__ state, NbrListsW L,
@@ -134,9 +192,7 @@ __global__ void __launch_bounds__(kSlotAlign) kDensity(const SceneDev* __restric
     const long long M = L.M;
     unsigned* __restrict__ nb = L.nbr + slot;
     unsigned* __restrict__ bnb = L.bnbr + slot;
-    unsigned* __restrict__ cnb = L.cnbr + slot;
-    int cS = 0, cW = 0, bc = 0, cc = 0;
-    float d = water ? pi4.w * S.W0 : 0.f;
+    int cS = 0, cW = 0, bc = 0;
     const int z0 = max(c.z - 1, 0), z1 = min(c.z + 1, S.gz - 1) + 1;
 #pragma unroll 1
     for (int dx = -1; dx <= 1; ++dx) {
@@ -148,35 +204,25 @@ __global__ void __launch_bounds__(kSlotAlign) kDensity(const SceneDev* __restric
             if (y < 0 || y >= S.gy) continue;
             const int base = S.cell_off + (x * S.gy + y) * S.gz;
             const unsigned jEnd = L.cs[base + z1];
-            // chunks of up to 32 candidates: a branch-free pass marks the
-            // candidates in reach, then the marked ones are appended in order
+            // chunks of up to 32 candidates: a branch-free pass shifts the
+            // sign of each candidate's reach test into a mask (candidate t
+            // ends at bit n-1-t), then the marked ones are appended in order
 #pragma unroll 1
             for (unsigned j0 = L.cs[base + z0]; j0 < jEnd; j0 += 32u) {
                 const int n = int(min(32u, jEnd - j0));
-                unsigned hit = 0u;
+                unsigned rev = 0u;
 #pragma unroll 4
                 for (int t = 0; t < n; ++t)
-                    hit |= unsigned(inReachFast(S, pi - xyz(pos4[j0 + unsigned(t)]))) << t;
+                    rev = __funnelshift_l(__float_as_uint(reachSign(S, pi - xyz(pos4[j0 + unsigned(t)]))), rev, 1);
+                unsigned hit = __brev(rev) >> (32 - n);
                 while (hit) {
                     const int t = __ffs(hit) - 1;
                     hit &= hit - 1u;
                     const unsigned j = j0 + unsigned(t);
-                    const float4 pj = pos4[j];
-                    const bool sandJ = pj.w < 0.f;
+                    const bool sandJ = pos4[j].w < 0.f;
                     if (cS + cW < L.cap) nb[(sandJ ? cS : L.cap - 1 - cW) * M] = j;
-                    if (sandJ) {
-                        ++cS;
-                        if (!water && j != unsigned(slot)) {
-                            const float3 dij = pi - xyz(pj);
-                            if (dot3(dij, dij) < S.dem_reach2) {
-                                if (cc < kMaxContact) cnb[cc * M] = j;
-                                ++cc;
-                            }
-                        }
-                    } else {
-                        ++cW;
-                        if (water) d += pj.w * poly6(S, len3(pi - xyz(pj)));  // label[i] == label[j]
-                    }
+                    cS += sandJ ? 1 : 0;
+                    cW += sandJ ? 0 : 1;
                 }
             }
             const unsigned bEnd = L.bcs[base + z1];
@@ -187,16 +233,43 @@ __global__ void __launch_bounds__(kSlotAlign) kDensity(const SceneDev* __restric
             }
         }
     }
-    // near walls the reference interleaves boundary terms cell by cell
-    if (water && bc > 0) d = exactDensity(S, L, pi, pi4.w, pos4, bpos4);
+    const bool listed = cS + cW <= L.cap;
+    int cc = 0;
+    if (!water) {
+        // sand-sand pairs within the DEM + liquid-bridge reach, in stencil order
+        unsigned* __restrict__ cnb = L.cnbr + slot;
+        auto contact = [&](unsigned j) {
+            if (j == unsigned(slot)) return;
+            const float3 dij = pi - xyz(pos4[j]);
+            if (dot3(dij, dij) < S.dem_reach2) {
+                if (cc < kMaxContact) cnb[cc * M] = j;
+                ++cc;
+            }
+        };
+        if (listed) {
+            for (int k = 0; k < cS; ++k) contact(nb[k * M]);
+        } else {
+            for (int x = max(c.x - 1, 0); x <= min(c.x + 1, S.gx - 1); ++x)
+                for (int y = max(c.y - 1, 0); y <= min(c.y + 1, S.gy - 1); ++y) {
+                    const int base = S.cell_off + (x * S.gy + y) * S.gz;
+                    for (unsigned j = L.cs[base + z0]; j < L.cs[base + z1]; ++j) {
+                        const float4 pj = pos4[j];
+                        if (pj.w < 0.f && inReachFast(S, pi - xyz(pj))) contact(j);
+                    }
+                }
+        }
+    }
     L.cnt[slot] = unsigned(min(cS, 0xFFFF)) | (unsigned(min(cW, 0xFFFF)) << 16);
     L.bcnt[slot] = bc;
-    L.ccnt[slot] = water ? 0 : cc;
+    L.ccnt[slot] = cc;
     float density, pressure = 0.f;
     if (!water) {
         density = S.rho1;
     } else {
-        density = d;
+        // the reference interleaves boundary terms cell by cell; without
+        // complete lists the stencil is walked again
+        density = listed && bc <= kMaxBNbr ? listDensity(S, L, slot, cW, bc, pi, pi4.w, pos4, bpos4)
+                                           : exactDensity(S, L, pi, pi4.w, pos4, bpos4);
         if (S.tait) {
             pressure = S.stiff * (powf(density / S.rho0, 7.f) - 1.f);
             if (pressure < 0.f) pressure *= S.neg_scale;
