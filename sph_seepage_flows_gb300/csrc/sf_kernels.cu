@@ -205,24 +205,29 @@ __global__ void __launch_bounds__(kSlotAlign) kDensity(const SceneDev* __restric
             const int base = S.cell_off + (x * S.gy + y) * S.gz;
             const unsigned jEnd = L.cs[base + z1];
             // chunks of up to 32 candidates: a branch-free pass shifts the
-            // sign of each candidate's reach test into a mask (candidate t
-            // ends at bit n-1-t), then the marked ones are appended in order
+            // sign of each candidate's reach test and its sand bit (the sign
+            // of w) into two masks (candidate t ends at bit n-1-t), then the
+            // marked ones are appended in order
 #pragma unroll 1
             for (unsigned j0 = L.cs[base + z0]; j0 < jEnd; j0 += 32u) {
                 const int n = int(min(32u, jEnd - j0));
-                unsigned rev = 0u;
+                unsigned rev = 0u, srev = 0u;
 #pragma unroll 4
-                for (int t = 0; t < n; ++t)
-                    rev = __funnelshift_l(__float_as_uint(reachSign(S, pi - xyz(pos4[j0 + unsigned(t)]))), rev, 1);
-                unsigned hit = __brev(rev) >> (32 - n);
-                while (hit) {
-                    const int t = __ffs(hit) - 1;
-                    hit &= hit - 1u;
-                    const unsigned j = j0 + unsigned(t);
-                    const bool sandJ = pos4[j].w < 0.f;
-                    if (cS + cW < L.cap) nb[(sandJ ? cS : L.cap - 1 - cW) * M] = j;
-                    cS += sandJ ? 1 : 0;
-                    cW += sandJ ? 0 : 1;
+                for (int t = 0; t < n; ++t) {
+                    const float4 q = pos4[j0 + unsigned(t)];
+                    rev = __funnelshift_l(__float_as_uint(reachSign(S, pi - xyz(q))), rev, 1);
+                    srev = __funnelshift_l(__float_as_uint(q.w), srev, 1);
+                }
+                const unsigned hit = __brev(rev) >> (32 - n), sand = __brev(srev) >> (32 - n);
+                // the list overflows when the two parts meet: from then on
+                // nothing reads it, so the order of the two appends is free
+                for (unsigned m = hit & sand; m; m &= m - 1u) {
+                    if (cS + cW < L.cap) nb[cS * M] = j0 + unsigned(__ffs(m) - 1);
+                    ++cS;
+                }
+                for (unsigned m = hit & ~sand; m; m &= m - 1u) {
+                    if (cS + cW < L.cap) nb[(L.cap - 1 - cW) * M] = j0 + unsigned(__ffs(m) - 1);
+                    ++cW;
                 }
             }
             const unsigned bEnd = L.bcs[base + z1];
@@ -238,23 +243,35 @@ __global__ void __launch_bounds__(kSlotAlign) kDensity(const SceneDev* __restric
     if (!water) {
         // sand-sand pairs within the DEM + liquid-bridge reach, in stencil order
         unsigned* __restrict__ cnb = L.cnbr + slot;
-        auto contact = [&](unsigned j) {
+        auto contact = [&](unsigned j, float3 pj) {
             if (j == unsigned(slot)) return;
-            const float3 dij = pi - xyz(pos4[j]);
+            const float3 dij = pi - pj;
             if (dot3(dij, dij) < S.dem_reach2) {
                 if (cc < kMaxContact) cnb[cc * M] = j;
                 ++cc;
             }
         };
         if (listed) {
-            for (int k = 0; k < cS; ++k) contact(nb[k * M]);
+            // indices and positions are loaded a group ahead (the entries
+            // were just written and come back from L2)
+            for (int k0 = 0; k0 < cS; k0 += 4) {
+                unsigned jj[4];
+                float3 pp[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) jj[u] = k0 + u < cS ? nb[(k0 + u) * M] : unsigned(slot);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) pp[u] = xyz(pos4[jj[u]]);
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (k0 + u < cS) contact(jj[u], pp[u]);
+            }
         } else {
             for (int x = max(c.x - 1, 0); x <= min(c.x + 1, S.gx - 1); ++x)
                 for (int y = max(c.y - 1, 0); y <= min(c.y + 1, S.gy - 1); ++y) {
                     const int base = S.cell_off + (x * S.gy + y) * S.gz;
                     for (unsigned j = L.cs[base + z0]; j < L.cs[base + z1]; ++j) {
                         const float4 pj = pos4[j];
-                        if (pj.w < 0.f && inReachFast(S, pi - xyz(pj))) contact(j);
+                        if (pj.w < 0.f && inReachFast(S, pi - xyz(pj))) contact(j, xyz(pj));
                     }
                 }
         }
