@@ -176,7 +176,10 @@ __device__ __forceinline__ float listDensity(const SceneDev& S, const NbrListsW&
 // order as the 27-cell loop with far fewer divergent loop exits. The walk
 // only appends list entries; the contact filter and the density sum then run
 // over the finished lists, where the lanes of a warp stay together.
-__global__ void __launch_bounds__(kSlotAlign) kDensity(const SceneDev* __restrict__ scenes,
+// The walk is bound by load latency: a register budget of 40 (6 blocks of
+// kSlotAlign threads per SM) buys occupancy that outweighs the few values it
+// moves to the stack.
+__global__ void __launch_bounds__(kSlotAlign, 6) kDensity(const SceneDev* __restrict__ scenes,
                                                        const int* __restrict__ blockScene,
                                                        SceneState* __restrict__ state, NbrListsW L,
                                                        const float4* __restrict__ pos4,
@@ -417,12 +420,15 @@ __global__ void __launch_bounds__(kSlotAlign) kVoidageAdhesion(
 }
 
 // ---------------------------------------------------------- sand momentum
+// Both momentum passes run with a register budget of 48 (5 blocks of
+// kSlotAlign threads per SM): their neighbour gathers are latency bound and
+// gain more from the occupancy than they lose to the values moved to the stack.
 // Compute[Multi]SFSandLinearMomentum_CUDA (cuda_sph_sf_solver_gpu.cuh:723-897):
 // DEM and capillary terms of sand neighbours (21-50, 83-109), buoyancy and
 // adhesion terms of water neighbours (240-273, 314-341), DEM against shape
 // boundary particles (52-81) and ComputeDemWorldBoundaryForces
 // (cuda_dem_solver_common_gpu.cuh:132-199). acc = g + 2 (f + df) / m.
-__global__ void __launch_bounds__(kSlotAlign) kSandMomentum(
+__global__ void __launch_bounds__(kSlotAlign, 5) kSandMomentum(
     const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene, NbrLists L,
     const float4* __restrict__ pos4, const float4* __restrict__ vel4, const float4* __restrict__ aux4,
     const float4* __restrict__ flow4, const float4* __restrict__ avgadh4, const float4* __restrict__ mat4,
@@ -513,7 +519,7 @@ __global__ void __launch_bounds__(kSlotAlign) kSandMomentum(
 // (cuda_sph_solver_common_gpu.cuh:89-139, called with rho0 as the particle
 // density). acc = g + (a - F_adh / m). Every thread then contributes |acc|
 // of its slot (sand included) to the scene maximum (cuda_wcsph_sf_solver.cu:43-47).
-__global__ void __launch_bounds__(kSlotAlign) kWaterMomentum(
+__global__ void __launch_bounds__(kSlotAlign, 5) kWaterMomentum(
     const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene, SceneState* __restrict__ state,
     NbrLists L, const float4* __restrict__ pos4, const float4* __restrict__ vel4, const float4* __restrict__ aux4,
     const float4* __restrict__ drag4, const float4* __restrict__ adh4, const float4* __restrict__ bpos4,
