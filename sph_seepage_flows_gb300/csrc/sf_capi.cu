@@ -922,6 +922,65 @@ int fieldWidth(int field) {
     }
 }
 
+// The xyz of one float4 slot array in sorted order <-> a packed n x 3 float
+// buffer (16-byte aligned), moved as whole 16-byte words through shared
+// memory: a block of 256 particles covers 192 words of the buffer, so pinned
+// host memory read or written over the host link sees full-line accesses
+// instead of three 4-byte accesses per particle.
+constexpr int kVecParticles = 256;
+__global__ void __launch_bounds__(kVecParticles) kGetVec3(int n, int slotOff, const float4* __restrict__ src,
+                                                          float4* __restrict__ out) {
+    __shared__ float4 buf4[kVecParticles * 3 / 4];
+    float* buf = reinterpret_cast<float*>(buf4);
+    const int t = threadIdx.x, p0 = blockIdx.x * kVecParticles, cnt = min(kVecParticles, n - p0);
+    if (t < cnt) {
+        const float4 v = src[slotOff + p0 + t];
+        buf[3 * t] = v.x;
+        buf[3 * t + 1] = v.y;
+        buf[3 * t + 2] = v.z;
+    }
+    __syncthreads();
+    float4* o = out + size_t(p0) * 3 / 4;  // p0 is a multiple of 4
+    const int words = 3 * cnt / 4, rem = 3 * cnt - 4 * words;
+    if (t < words) o[t] = buf4[t];
+    if (t < rem) reinterpret_cast<float*>(o + words)[t] = buf[4 * words + t];
+}
+__global__ void __launch_bounds__(kVecParticles) kSetVec3(int n, int slotOff, float4* __restrict__ dst,
+                                                          const float4* __restrict__ in) {
+    __shared__ float4 buf4[kVecParticles * 3 / 4];
+    float* buf = reinterpret_cast<float*>(buf4);
+    const int t = threadIdx.x, p0 = blockIdx.x * kVecParticles, cnt = min(kVecParticles, n - p0);
+    const float4* src = in + size_t(p0) * 3 / 4;
+    const int words = 3 * cnt / 4, rem = 3 * cnt - 4 * words;
+    if (t < words) buf4[t] = src[t];
+    if (t < rem) buf[4 * words + t] = reinterpret_cast<const float*>(src + words)[t];
+    __syncthreads();
+    if (t < cnt) {
+        float4 v = dst[slotOff + p0 + t];
+        v.x = buf[3 * t];
+        v.y = buf[3 * t + 1];
+        v.z = buf[3 * t + 2];
+        dst[slotOff + p0 + t] = v;
+    }
+}
+
+// The float4 slot array whose xyz is field (3-wide float fields), else null.
+float4* vec3Array(sf_handle* h, int field) {
+    const int c = h->cur;
+    switch (field) {
+    case SF_FIELD_POS: return h->pos[c];
+    case SF_FIELD_VEL: return h->vel[c];
+    case SF_FIELD_ACC: return h->acc;
+    case SF_FIELD_COL: return h->col[c];
+    case SF_FIELD_AVG_FLOW: return h->flow;
+    case SF_FIELD_AVG_DRAG: return h->drag;
+    case SF_FIELD_ADHESION: return h->adh;
+    case SF_FIELD_AVG_ADHESION: return h->avgadh;
+    case SF_FIELD_CDA0ASAT: return h->mat[c];
+    default: return nullptr;
+    }
+}
+
 // Device address of page-locked (pinned) host memory, which kernels can
 // read and write directly over the host link; nullptr for other memory.
 void* mappedHostPointer(const void* p) {
@@ -987,7 +1046,11 @@ sf_status sf_get_field(sf_handle* h, int32_t scene, int32_t field, int32_t order
         }
     }
     const int blocks = int((n + 255) / 256);
-    if (bfield) {
+    float4* vec = bfield || order != SF_ORDER_SORTED ? nullptr : vec3Array(h, field);
+    if (vec && (reinterpret_cast<uintptr_t>(target) & 15u) == 0) {
+        kGetVec3<<<int((n + kVecParticles - 1) / kVecParticles), kVecParticles, 0, h->stream>>>(
+            int(n), S.slot_off, vec, static_cast<float4*>(target));
+    } else if (bfield) {
         kGetBoundary<<<blocks, 256, 0, h->stream>>>(field, int(n), S.b_off, h->bpos, h->blabel, target);
     } else {
         const int c = h->cur;
@@ -1033,9 +1096,15 @@ sf_status sf_set_field(sf_handle* h, int32_t scene, int32_t field, int32_t order
         }
     }
     const int c = h->cur;
-    kSetField<<<int((n + 255) / 256), 256, 0, h->stream>>>(field, int(n), S.slot_off, order, h->pos[c], h->vel[c],
-                                                           h->col[c], h->mat[c], h->amc[c], h->pid[c], h->aux,
-                                                           h->flow, h->adh, h->avgadh, h->drag, h->acc, from);
+    float4* vec = order == SF_ORDER_SORTED ? vec3Array(h, field) : nullptr;
+    if (vec && (reinterpret_cast<uintptr_t>(from) & 15u) == 0)
+        kSetVec3<<<int((n + kVecParticles - 1) / kVecParticles), kVecParticles, 0, h->stream>>>(
+            int(n), S.slot_off, vec, static_cast<const float4*>(from));
+    else
+        kSetField<<<int((n + 255) / 256), 256, 0, h->stream>>>(field, int(n), S.slot_off, order, h->pos[c],
+                                                               h->vel[c], h->col[c], h->mat[c], h->amc[c], h->pid[c],
+                                                               h->aux, h->flow, h->adh, h->avgadh, h->drag, h->acc,
+                                                               from);
     if (h->cuda(cudaGetLastError(), "set_field launch")) return SF_ERR_CUDA;
     if (!src_on_device) return h->cuda(cudaStreamSynchronize(h->stream), "set_field sync");
     return SF_OK;
