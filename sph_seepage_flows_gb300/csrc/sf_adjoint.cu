@@ -481,13 +481,7 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjSandSelf(const SceneDev* __res
         const float3 xk = xyz(pk4), vk = xyz(b.vel4[slot]);
         const float rhoK = b.vel4[slot].w, epsK = b.aux4[slot].w;
         const float tanPhi = sqrtf(S.tan2);
-        float vw = 0.f;
-        LabelCursor<false> wc(S, b.lists, slot, xk, b.pos4);
-        for (int j; wc.next(j);) {
-            const float4 pj4 = b.pos4[j];
-            const float ej = b.aux4[j].w;
-            if (ej > 0.f && ej <= 1.f) vw += pj4.w / (b.vel4[j].w / fmaxf(kEps, ej)) * poly6(S, len3(xk - xyz(pj4)));
-        }
+        const float vw = b.dp[slot].y;  // stored by the forward
         const float3 fb = (2.f / mk) * xyz(A.acc[slot]);
         const float3 dragB = xyz(A.drag[slot]);
         // df; seeds eps 0, flow 1-3, v 4-6, permeability scale 7
@@ -656,26 +650,14 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjVoidSelf(const SceneDev* __res
     if (pk4.w == 0.f) return;
     const float3 xk = xyz(pk4);
     if (pk4.w < 0.f) {
-        float num = 0.f, den = 0.f;
-        LabelCursor<false> wc(S, b.lists, slot, xk, b.pos4);
-        for (int j; wc.next(j);) {
-            const float4 pj4 = b.pos4[j];
-            const float vj = pj4.w / b.vel4[j].w;
-            const float wij = poly6(S, len3(xk - xyz(pj4)));
-            num += b.aux4[j].y * vj * wij;
-            den += vj * wij;
-        }
+        // voidage = num / den, with den and the quotient stored by the forward
+        const float den = b.dp[slot].x;
         // quotient rule without squaring den (a small den would underflow)
         const float eb = A.s[slot].z;
-        A.r[slot] = den != 0.f ? make_float4(eb / den, -(eb / den) * (num / den), 0.f, 0.f)
+        A.r[slot] = den != 0.f ? make_float4(eb / den, -(eb / den) * b.aux4[slot].w, 0.f, 0.f)
                                : make_float4(0.f, 0.f, 0.f, 0.f);
     } else {
-        float vs = 0.f;
-        LabelCursor<true> sc(S, b.lists, slot, xk, b.pos4);
-        for (int j; sc.next(j);) {
-            const float4 pj4 = b.pos4[j];
-            vs += -pj4.w / b.vel4[j].w * poly6(S, len3(xk - xyz(pj4)));
-        }
+        const float vs = b.adh4[slot].w;  // stored by the forward
         const float3 avgB = xyz(A.avgadh[slot]);
         float3 tot = xyz(A.adh[slot]);
         float vsb = 0.f;

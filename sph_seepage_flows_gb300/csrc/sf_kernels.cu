@@ -382,6 +382,7 @@ __global__ void __launch_bounds__(kSlotAlign) kVoidageAdhesion(
             den += vj * wij;
         });
         aux4[slot].w = den != 0.f ? num / den : 0.f;
+        dp[slot] = make_float2(den, 0.f);  // the quotient's denominator, for the adjoint
         // wet-sand colour ratchet
         float4 c = col4[slot];
         if (c.w < sat) {
@@ -408,7 +409,7 @@ __global__ void __launch_bounds__(kSlotAlign) kVoidageAdhesion(
             const float vj = mj / vel4[j].w;
             v_s += vj * wij;
         });
-        adh4[slot] = make_float4(ad.x, ad.y, ad.z, 0.f);
+        adh4[slot] = make_float4(ad.x, ad.y, ad.z, v_s);  // w: the average's denominator, for the adjoint
         const float3 avg = v_s != 0.f ? ad / v_s : mk3(0.f, 0.f, 0.f);
         avgadh4[slot] = make_float4(avg.x, avg.y, avg.z, 0.f);
         // the effective density and pressure term, with the operations every
@@ -432,7 +433,7 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kSandMomentum(
     const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene, NbrLists L,
     const float4* __restrict__ pos4, const float4* __restrict__ vel4, const float4* __restrict__ aux4,
     const float4* __restrict__ flow4, const float4* __restrict__ avgadh4, const float4* __restrict__ mat4,
-    const float4* __restrict__ bpos4, const float2* __restrict__ dp, float4* __restrict__ drag4,
+    const float4* __restrict__ bpos4, float2* __restrict__ dp, float4* __restrict__ drag4,
     float4* __restrict__ acc4) {
     SF_SLOT_PROLOGUE
     const float4 pi4 = pos4[slot];
@@ -507,6 +508,7 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kSandMomentum(
     }
     const float3 avgDrag = v_w != 0.f ? df / v_w : mk3(0.f, 0.f, 0.f);
     drag4[slot] = make_float4(avgDrag.x, avgDrag.y, avgDrag.z, 0.f);
+    reinterpret_cast<float*>(dp + slot)[1] = v_w;  // the average's denominator, for the adjoint
     const float3 g = mk3(0.f, 0.f, 0.f) + mk3(S.gvx, S.gvy, S.gvz);
     const float3 a = g + 2.f * (f + df) / mi;
     acc4[slot] = make_float4(a.x, a.y, a.z, 0.f);

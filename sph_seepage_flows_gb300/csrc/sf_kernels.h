@@ -80,7 +80,11 @@ struct PassBuffers {
     const float4* bpos4;
     // water: (D, P) = (rho / max(eps, voidage), p / max(eps, D^2)), the
     // effective density and pressure term every momentum pair term of the
-    // particle uses (written by the voidage / adhesion pass)
+    // particle uses (written by the voidage / adhesion pass); sand: the
+    // denominators of its voidage quotient and of its average drag (written
+    // by the voidage and sand momentum passes), which the adjoint reads
+    // instead of summing them again. adh4.w of water holds the denominator
+    // of its average adhesion for the same reason.
     float2* dp;
 };
 
