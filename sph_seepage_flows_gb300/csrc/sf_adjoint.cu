@@ -21,9 +21,9 @@
 // a_j(j,k) = -(m_k / m_j) a_k(k,j); sand contacts: f_j(j,k) = -f_k(k,j))
 // are evaluated once per thread with the combined cotangent of both ends.
 //
-// The vector-Jacobian products of the SPH kernels and of the water, seepage,
-// boundary and sand-water terms are written out by hand below; the DEM +
-// capillary contact, the wall forces, the drag and the adhesion use
+// The vector-Jacobian products of the SPH kernels, of the water, seepage,
+// boundary and sand-water terms and of the water adhesion are written out by
+// hand below; the DEM + capillary contact, the wall forces and the drag use
 // forward-mode dual numbers (sf_dual.cuh) over their few inputs. Branch
 // conditions (contact, friction cap, damping sign, positive voidage, water
 // clamp, viscosity switch) are taken from the forward values.
@@ -281,11 +281,39 @@ __device__ __forceinline__ V3T<T> dragT(const SceneDev& S, T eps, V3T<T> flow, V
     if (val(dragCoeff) == 0.f) return v * 0.f;
     return ((S.grav_abs * S.rho0) * tpow(eps, 2.f) / dragCoeff) * (flow - v) * m / rho;
 }
-// Adhesion on water i from sand j (175-207, 574-678); d = x_i - x_j.
-template <typename T>
-__device__ __forceinline__ V3T<T> adhesionT(const SceneDev& S, V3T<T> d, T satJ, float mi, float mj) {
-    const T l = lenT(d);
-    return (bezierT(S.adhG, satJ, 1.f) * mi * mj * adhesionSplineT(S, l)) * d / tmaxc(kEps, l);
+// Derivative of QuadraticBezierCoeff (cuda_sf_utils.cuh:57-82) in sr, branch
+// by branch: first segment dB/dt = 2 (1 - t)(py1 - py0) with t = sr / px1;
+// second segment dB/dt = 2 t (py2 - py1) with t = (b + sqrt(c + d (px1 - sr))) / e.
+__device__ __forceinline__ float bezierDeriv(const BezierDev& G, float sr) {
+    if (sr < 0.f || sr >= 1.f) return 0.f;
+    if (sr <= G.px1) return 2.f * (1.f - sr / G.px1) * (G.py1 - G.py0) / G.px1;
+    const float root = sqrtf(G.c + G.d * (G.px1 - sr));
+    const float t = (G.b + root) / G.e;
+    return 2.f * t * (G.py2 - G.py1) * (-G.d / (2.f * G.e * root));
+}
+
+// Vector-Jacobian product of the adhesion on water i from sand j,
+// F = B(sat_j) m_i m_j A(l) d / l (d = x_i - x_j, l = |d| in (h/2, h], where
+// the Akinci spline A is non-zero): with g = A / l,
+//   u^T dF/dd = B m_i m_j (g u + g'(l) (d.u / l) d),  g' = A'(l) / l - A / l^2,
+//   u^T dF/dsat_j = B'(sat_j) m_i m_j g (d.u),
+// A = c q^(1/4) with q = -4 l^2 / h + 6 l - 2 h, A' = c q^(-3/4) (6 - 8 l / h) / 4.
+__device__ __forceinline__ void adhesionVjp(const SceneDev& S, float3 d, float satJ, float mi, float mj, float3 u,
+                                            float3& gd, float& gsat) {
+    const float l2 = dot3(d, d), l = sqrtf(l2);
+    gd = mk3(0.f, 0.f, 0.f);
+    gsat = 0.f;
+    if (!(2.f * l > S.h && l <= S.h)) return;
+    const float q = -4.f * l * l / S.h + 6.f * l - 2.f * S.h;
+    const float A = S.adh_coef * powf(q, 0.25f);
+    // dA/dl = adh_coef q^(-3/4) (6 - 8l/h) / 4, taken as 0 at q = 0 (l = h)
+    const float dAdl = q != 0.f ? 0.25f * S.adh_coef * powf(q, -0.75f) * (6.f - 8.f * l / S.h) : 0.f;
+    const float m = mi * mj;
+    const float du = dot3(d, u);
+    const float g = A / l;
+    const float gp = dAdl / l - A / l2;
+    gd = (bezier(S.adhG, satJ) * m) * (g * u + (gp * du / l) * d);
+    gsat = bezierDeriv(S.adhG, satJ) * m * g * du;
 }
 
 // ------------------------------------------------------------- kernels
@@ -696,9 +724,11 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjVoidPairs(const SceneDev* __re
             // k in the adhesion and v_s of water j; seeds d 0-2, sat_k 3
             const float4 rj = A.r[j];
             if (2.f * dot3(d, d) > 0.5f * S.h2) {  // the adhesion spline vanishes for |d| <= h / 2
-                const auto o = adhesionT<Dual<4>>(S, dvec<4>(d, 0), dseed<4>(satK, 3), pj4.w, mk);
-                gx -= vjp3(xyz(rj), o, 0);
-                gsat += vjp(xyz(rj), o, 3);
+                float3 gd;
+                float gs;
+                adhesionVjp(S, d, satK, pj4.w, mk, xyz(rj), gd, gs);
+                gx -= gd;
+                gsat += gs;
             }
             gx -= (rj.w * vk) * gW;
         }
@@ -714,8 +744,12 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjVoidPairs(const SceneDev* __re
             const float3 d = xk - xyz(pj4);
             const float3 gW = poly6Grad(S, d);
             // own adhesion and v_s terms
-            if (2.f * dot3(d, d) > 0.5f * S.h2)
-                gx += vjp3(xyz(rk), adhesionT<Dual<3>>(S, dvec<3>(d, 0), dconst<3>(b.aux4[j].z), mk, -pj4.w), 0);
+            if (2.f * dot3(d, d) > 0.5f * S.h2) {
+                float3 gd;
+                float gs;
+                adhesionVjp(S, d, b.aux4[j].z, mk, -pj4.w, xyz(rk), gd, gs);
+                gx += gd;
+            }
             gx += (rk.w * (-pj4.w / b.vel4[j].w)) * gW;
             // k in num / den of sand j: (e_f,k n + m) V_k W(x_j - x_k), V_k = m_k / rho_k
             const float4 rj = A.r[j];

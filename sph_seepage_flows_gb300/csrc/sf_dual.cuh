@@ -148,10 +148,6 @@ template <typename T> __device__ __forceinline__ V3T<T> spikyGradT(const SceneDe
     T d = S.h - rl;
     return (S.spiky * d * d / rl) * r;
 }
-template <typename T> __device__ __forceinline__ T adhesionSplineT(const SceneDev& S, T r) {
-    if (2.f * val(r) > S.h && val(r) <= S.h) return S.adh_coef * tpow(-4.f * r * r / S.h + 6.f * r - 2.f * S.h, 0.25f);
-    return r * 0.f;
-}
 template <typename T> __device__ __forceinline__ T bezierT(const BezierDev& G, T sr, float scale) {
     if (val(sr) < 0.f) return sr * 0.f + scale * G.py0;
     if (val(sr) >= 1.f) return sr * 0.f + scale * G.py2;
