@@ -250,12 +250,6 @@ __device__ __forceinline__ float3 chainPressureTerm(float Pbar, float Dbar, floa
 }
 
 // ------------------------------------------ dual-number pair terms
-// DEM + capillary force on sand i from sand j (21-50, 83-109); d = x_j - x_i, dv = v_j - v_i.
-template <typename T>
-__device__ __forceinline__ V3T<T> contactT(const SceneDev& S, V3T<T> d, V3T<T> dv, T satI, T satJ, T tanPhi,
-                                           T capScale) {
-    return demForceT(d, dv, S.rij2, S.kn, S.ks, tanPhi * tanPhi) + capillaryForceT(S, d, (satI + satJ) / 2.f, capScale);
-}
 // ComputeDemWorldBoundaryForces on sand i (cuda_dem_solver_common_gpu.cuh:132-199).
 template <typename T>
 __device__ __forceinline__ V3T<T> wallsT(const SceneDev& S, V3T<T> p, V3T<T> v, T tanPhi) {
@@ -597,14 +591,25 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjSandPairs(const SceneDev* __re
                 }
                 const float3 d = xyz(b.pos4[j]) - xk;
                 const float3 c = fb - xyz(A.f[j]);
-                // seeds d 0-2, dv 3-5, sat_k 6, tan phi 7, capillary scale 8
-                const auto o = contactT<Dual<9>>(S, dvec<9>(d, 0), dvec<9>(xyz(b.vel4[j]) - vk, 3), dseed<9>(satK, 6),
-                                                 dconst<9>(b.aux4[j].z), dseed<9>(tanPhi, 7), dseed<9>(1.f, 8));
-                gx -= vjp3(c, o, 0);
-                gv -= vjp3(c, o, 3);
-                gsat += vjp(c, o, 6);
-                gTan += vjp(fb, o, 7);
-                gCap += vjp(fb, o, 8);
+                // DEM acts while the spheres overlap (dist < 2r), the liquid
+                // bridge only at gaps 0 < H < rupture: at most one of the two
+                // is non-zero, so each gets its own narrower dual evaluation
+                const float dist = len3(d);
+                if (S.rij2 - dist > 0.f) {
+                    // seeds d 0-2, dv 3-5, tan phi 6
+                    const auto tp = dseed<7>(tanPhi, 6);
+                    const auto o = demForceT(dvec<7>(d, 0), dvec<7>(xyz(b.vel4[j]) - vk, 3), S.rij2, S.kn, S.ks, tp * tp);
+                    gx -= vjp3(c, o, 0);
+                    gv -= vjp3(c, o, 3);
+                    gTan += vjp(fb, o, 6);
+                } else if (dist - (S.dem_radius + S.dem_radius) < S.cap_srupt) {
+                    // seeds d 0-2, sat_k 3, capillary scale 4
+                    const auto o = capillaryForceT(S, dvec<5>(d, 0), (dseed<5>(satK, 3) + b.aux4[j].z) / 2.f,
+                                                   dseed<5>(1.f, 4));
+                    gx -= vjp3(c, o, 0);
+                    gsat += vjp(c, o, 3);
+                    gCap += vjp(fb, o, 4);
+                }
             }
             const float volK = mk / fmaxf(kEps, rhoK);
             LabelCursor<false> wc(S, L, slot, xk, b.pos4);
