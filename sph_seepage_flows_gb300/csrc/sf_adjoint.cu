@@ -46,23 +46,49 @@ namespace sfg {
     const int sid = blockScene[(blockIdx.x * blockDim.x) / kSlotAlign];    \
     const SceneDev& S = scenes[sid];
 
+// Pair kernels run G consecutive threads (lanes of one warp) per slot: lane
+// `part` takes neighbour entries part, part + G, ... and the per-slot sums
+// are reduced over the G lanes before lane 0 writes them. Small scenes have
+// too few slots to hide the latency of one long neighbour loop per thread;
+// G = 1 is the one-thread-per-slot layout of large scenes.
+#define SF_ADJ_PROLOGUE_G                                                     \
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;                    \
+    const int slot = gid / G, part = gid % G;                                 \
+    const int sid = blockScene[(blockIdx.x * (blockDim.x / G)) / kSlotAlign]; \
+    const SceneDev& S = scenes[sid];
+
+// Sum over the G lanes of a slot (G divides 32; all G lanes call it).
+template <int G> __device__ __forceinline__ float groupSum(float v) {
+    if (G > 1) {
+        const unsigned lane = threadIdx.x & 31u;
+        const unsigned mask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << (lane & ~unsigned(G - 1));
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+    }
+    return v;
+}
+template <int G> __device__ __forceinline__ float3 groupSum3(float3 v) {
+    return make_float3(groupSum<G>(v.x), groupSum<G>(v.y), groupSum<G>(v.z));
+}
+
 // ------------------------------------------------------ neighbour cursors
 // The neighbours of one label (list, or the stencil when the list
 // overflowed) from a single call site, so that the loop body is inlined.
-template <bool kSand> struct LabelCursor {
+template <bool kSand, int G = 1> struct LabelCursor {
     const SceneDev* S;
     const unsigned* cs;
     const float4* pos4;
     const unsigned* p;
     long long step;
     float3 pi;
-    int n, k, x, x1, y, y0, y1, z0, z1;
-    unsigned j, jEnd;
+    int n, k, x, x1, y, y0, y1, z0, z1, part;
+    unsigned j, jEnd, hits;
     bool stencil;
 
+    // part in [0, G): this lane's share, every G-th neighbour from the part-th
     __device__ __forceinline__ LabelCursor(const SceneDev& s, const NbrLists& L, int slot, float3 p_i,
-                                           const float4* __restrict__ pos)
-        : S(&s), cs(L.cs), pos4(pos), pi(p_i), k(0), j(0), jEnd(0) {
+                                           const float4* __restrict__ pos, int part_ = 0)
+        : S(&s), cs(L.cs), pos4(pos), pi(p_i), k(part_), part(part_), j(0), jEnd(0), hits(0) {
         const unsigned c = L.cnt[slot];
         stencil = int(c & 0xFFFFu) + int(c >> 16) > L.cap;
         n = kSand ? int(c & 0xFFFFu) : int(c >> 16);
@@ -84,7 +110,7 @@ template <bool kSand> struct LabelCursor {
         if (!stencil) {
             if (k >= n) return false;
             out = int(p[k * step]);
-            ++k;
+            k += G;
             return true;
         }
         for (;;) {
@@ -92,6 +118,7 @@ template <bool kSand> struct LabelCursor {
                 const unsigned c = j++;
                 const float4 pj = pos4[c];
                 if ((kSand ? pj.w < 0.f : pj.w > 0.f) && inReach(*S, pi - xyz(pj))) {
+                    if (G > 1 && int(hits++ % unsigned(G)) != part) continue;
                     out = int(c);
                     return true;
                 }
@@ -108,20 +135,21 @@ template <bool kSand> struct LabelCursor {
 };
 
 // Boundary particles within reach (list, or the boundary stencil on overflow).
-struct BoundaryCursor {
+template <int G = 1> struct BoundaryCursor {
     const SceneDev* S;
     const unsigned* bcs;
     const float4* bpos4;
     const unsigned* p;
     long long M;
     float3 pi;
-    int n, k, x, x1, y, y0, y1, z0, z1;
-    unsigned j, jEnd;
+    int n, k, x, x1, y, y0, y1, z0, z1, part;
+    unsigned j, jEnd, hits;
     bool stencil;
 
     __device__ __forceinline__ BoundaryCursor(const SceneDev& s, const NbrLists& L, int slot, float3 p_i,
-                                              const float4* __restrict__ bpos)
-        : S(&s), bcs(L.bcs), bpos4(bpos), p(L.bnbr + slot), M(L.M), pi(p_i), k(0), j(0), jEnd(0) {
+                                              const float4* __restrict__ bpos, int part_ = 0)
+        : S(&s), bcs(L.bcs), bpos4(bpos), p(L.bnbr + slot), M(L.M), pi(p_i), k(part_), part(part_), j(0), jEnd(0),
+          hits(0) {
         n = L.bcnt[slot];
         stencil = n > kMaxBNbr;
         x = x1 = y = y0 = y1 = z0 = z1 = 0;
@@ -140,13 +168,14 @@ struct BoundaryCursor {
         if (!stencil) {
             if (k >= n) return false;
             out = int(p[size_t(k) * size_t(M)]);
-            ++k;
+            k += G;
             return true;
         }
         for (;;) {
             while (j < jEnd) {
                 const unsigned c = j++;
                 if (inReach(*S, pi - xyz(bpos4[c]))) {
+                    if (G > 1 && int(hits++ % unsigned(G)) != part) continue;
                     out = int(c);
                     return true;
                 }
@@ -376,10 +405,11 @@ __global__ void kAdjIntegrate(const SceneDev* __restrict__ scenes, const int* __
 //   T = -(P_k + P_j) G(d) - [dv.d < 0] Pi G(d),  Pi = kappa dv.d / (d.d + eps),
 //   kappa = -nu / (D_k + D_j),  D = rho / max(eps, e),  P = p / max(eps, D^2),
 // so both ends are served by the cotangent c = m_j a-bar_k - m_k a-bar_j on T.
+template <int G>
 __global__ void __launch_bounds__(kSlotAlign) kAdjWater(const SceneDev* __restrict__ scenes,
                                                         const int* __restrict__ blockScene, AdjBuffers A,
                                                         PassBuffers b) {
-    SF_ADJ_PROLOGUE
+    SF_ADJ_PROLOGUE_G
     const float4 pk4 = b.pos4[slot];
     if (pk4.w == 0.f) return;
     const NbrLists& L = b.lists;
@@ -391,12 +421,12 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjWater(const SceneDev* __restri
     if (pk4.w > 0.f) {
         const float mk = pk4.w;
         const float3 ak = xyz(A.acc[slot]);
-        A.adh[slot] = f4(ak / -mk);
+        if (part == 0) A.adh[slot] = f4(ak / -mk);
         const float2 dpk = b.dp[slot];
         const float Dk = dpk.x;
         const float Pk = dpk.y;
         float Pbar = 0.f, Dbar = 0.f, pbar = 0.f;
-        LabelCursor<false> wc(S, L, slot, xk, b.pos4);
+        LabelCursor<false, G> wc(S, L, slot, xk, b.pos4, part);
         for (int j; wc.next(j);) {
             if (j == slot) continue;
             const float4 pj4 = b.pos4[j];
@@ -425,7 +455,7 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjWater(const SceneDev* __restri
             gx += coef * spikyVjp(sp, d, c);
         }
         // seepage terms of sand j: (-m_j p_k / max(eps, D_k rho_j)) G(d) - W(d) / D_k drag_j
-        LabelCursor<true> sc(S, L, slot, xk, b.pos4);
+        LabelCursor<true, G> sc(S, L, slot, xk, b.pos4, part);
         for (int j; sc.next(j);) {
             const float4 pj4 = b.pos4[j];
             const float3 d = xk - xyz(pj4);
@@ -442,7 +472,7 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjWater(const SceneDev* __restri
         // boundary pressure and viscosity (rho0 as the density)
         const float gam0 = -S.rho0 / fmaxf(kEps, S.rho0 * S.rho0);
         const float kb = -S.bnu / (2.f * S.rho0);
-        BoundaryCursor bc(S, L, slot, xk, b.bpos4);
+        BoundaryCursor<G> bc(S, L, slot, xk, b.bpos4, part);
         for (int bb; bc.next(bb);) {
             const float4 bj = b.bpos4[bb];
             const float vol = fabsf(bj.w);
@@ -462,18 +492,23 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjWater(const SceneDev* __restri
             }
             gx += coef * spikyVjp(sp, d, ak);
         }
-        const float3 s3 = chainPressureTerm(Pbar, Dbar, pK, rhoK, epsK);
-        float4 s = A.s[slot];
-        s.x += s3.x;
-        s.y += s3.y + pbar;
-        s.z += s3.z;
-        A.s[slot] = s;
+        Pbar = groupSum<G>(Pbar);
+        Dbar = groupSum<G>(Dbar);
+        pbar = groupSum<G>(pbar);
+        if (part == 0) {
+            const float3 s3 = chainPressureTerm(Pbar, Dbar, pK, rhoK, epsK);
+            float4 s = A.s[slot];
+            s.x += s3.x;
+            s.y += s3.y + pbar;
+            s.z += s3.z;
+            A.s[slot] = s;
+        }
     } else {
         // sand k in the seepage term of water i: d = x_i - x_k
         const float mk = -pk4.w;
         const float3 dragK = xyz(b.drag4[slot]);
         float3 gdrag = mk3(0.f, 0.f, 0.f);
-        LabelCursor<false> wc(S, L, slot, xk, b.pos4);
+        LabelCursor<false, G> wc(S, L, slot, xk, b.pos4, part);
         for (int i; wc.next(i);) {
             const float4 pi4 = b.pos4[i];
             const float3 d = xyz(pi4) - xk;
@@ -484,17 +519,23 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjWater(const SceneDev* __restri
             gx -= alpha * spikyVjp(sp, d, ai) + (-dot3(ai, dragK) / Di) * poly6Grad(S, d);
             gdrag += (-poly6(S, len3(d)) / Di) * ai;
         }
-        A.drag[slot] = f4(gdrag);
+        gdrag = groupSum3<G>(gdrag);
+        if (part == 0) A.drag[slot] = f4(gdrag);
     }
+    gx = groupSum3<G>(gx);
+    gv = groupSum3<G>(gv);
+    if (part != 0) return;
     add3(A.x[slot], gx);
     add3(A.v[slot], gv);
 }
 
 // A3a: per sand particle: v_w, drag, walls and shape-boundary DEM; writes
 // (f-bar, v_w-bar) and adds the friction / permeability parameter partials.
+// paramPartial: 3 floats per block of the lane-split pair kernels (G blocks
+// per block of this kernel); this block adds into the first of its G.
 __global__ void __launch_bounds__(kSlotAlign) kAdjSandSelf(const SceneDev* __restrict__ scenes,
                                                            const int* __restrict__ blockScene, AdjBuffers A,
-                                                           PassBuffers b, float* __restrict__ paramPartial) {
+                                                           PassBuffers b, float* __restrict__ paramPartial, int G) {
     SF_ADJ_PROLOGUE
     const float4 pk4 = b.pos4[slot];
     float gTan = 0.f, gPerm = 0.f;
@@ -526,7 +567,7 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjSandSelf(const SceneDev* __res
         gv += vjp3(fb, w, 3);
         gTan = vjp(fb, w, 6);
         if (S.shape_boundary) {
-            BoundaryCursor bc(S, b.lists, slot, xk, b.bpos4);
+            BoundaryCursor<> bc(S, b.lists, slot, xk, b.bpos4);
             for (int bb; bc.next(bb);) {
                 const float4 bj = b.bpos4[bb];
                 if (!(bj.w < 0.f)) continue;
@@ -543,8 +584,8 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjSandSelf(const SceneDev* __res
     }
     const float2 t = blockSum2(gTan, gPerm);
     if (threadIdx.x == 0) {
-        paramPartial[3 * blockIdx.x] += t.x;
-        paramPartial[3 * blockIdx.x + 2] += t.y;
+        paramPartial[3 * size_t(blockIdx.x) * G] += t.x;
+        paramPartial[3 * size_t(blockIdx.x) * G + 2] += t.y;
     }
 }
 
@@ -553,10 +594,11 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjSandSelf(const SceneDev* __res
 // the sand end and from the water end:
 //   f_i += [0 < e_j <= 1] (-m_i m_j p_j / max(eps, rho_i D_j)) G(x_i - x_j) + W vol_i avgadh_j,
 //   v_w,i += [0 < e_j <= 1] (m_j / D_j) W(x_i - x_j).
+template <int G>
 __global__ void __launch_bounds__(kSlotAlign) kAdjSandPairs(const SceneDev* __restrict__ scenes,
                                                             const int* __restrict__ blockScene, AdjBuffers A,
                                                             PassBuffers b, float* __restrict__ paramPartial) {
-    SF_ADJ_PROLOGUE
+    SF_ADJ_PROLOGUE_G
     const float4 pk4 = b.pos4[slot];
     float gTan = 0.f, gCap = 0.f;
     if (pk4.w != 0.f) {
@@ -577,8 +619,8 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjSandPairs(const SceneDev* __re
             // contacts: the contact list, or the sand list filtered by the DEM reach
             const int ncon = L.ccnt[slot];
             const bool filtered = ncon > kMaxContact;
-            LabelCursor<true> sc(S, L, slot, xk, b.pos4);
-            for (int k = 0;; ++k) {
+            LabelCursor<true, G> sc(S, L, slot, xk, b.pos4, part);
+            for (int k = part;; k += G) {
                 int j;
                 if (!filtered) {
                     if (k >= ncon) break;
@@ -612,7 +654,7 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjSandPairs(const SceneDev* __re
                 }
             }
             const float volK = mk / fmaxf(kEps, rhoK);
-            LabelCursor<false> wc(S, L, slot, xk, b.pos4);
+            LabelCursor<false, G> wc(S, L, slot, xk, b.pos4, part);
             for (int j; wc.next(j);) {
                 const float4 pj4 = b.pos4[j];
                 const float3 d = xk - xyz(pj4);
@@ -625,7 +667,8 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjSandPairs(const SceneDev* __re
                     gx += sigma * spikyVjp(spikyD(S, d), d, fb) + (vwb * pj4.w / Dj) * gW;
                 }
             }
-            A.s[slot].w += gsat;
+            gsat = groupSum<G>(gsat);
+            if (part == 0) A.s[slot].w += gsat;
         } else {
             // water k in the terms of sand i: d = x_i - x_k
             const float mk = pk4.w;
@@ -634,7 +677,7 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjSandPairs(const SceneDev* __re
             const float Dk = rhoK / fmaxf(kEps, epsK);
             float3 gadh = mk3(0.f, 0.f, 0.f);
             float pbar = 0.f, Dbar = 0.f;
-            LabelCursor<true> sc(S, L, slot, xk, b.pos4);
+            LabelCursor<true, G> sc(S, L, slot, xk, b.pos4, part);
             for (int i; sc.next(i);) {
                 const float4 pi4 = b.pos4[i];
                 const float4 fi4 = A.f[i];
@@ -656,15 +699,24 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjSandPairs(const SceneDev* __re
                     Dbar += fi4.w * (-mk * W / (Dk * Dk));
                 }
             }
-            add3(A.avgadh[slot], gadh);
-            float4 s = A.s[slot];
-            s.x += Dbar / fmaxf(kEps, epsK);
-            s.y += pbar;
-            if (epsK > kEps) s.z += Dbar * (-rhoK / (epsK * epsK));
-            A.s[slot] = s;
+            gadh = groupSum3<G>(gadh);
+            pbar = groupSum<G>(pbar);
+            Dbar = groupSum<G>(Dbar);
+            if (part == 0) {
+                add3(A.avgadh[slot], gadh);
+                float4 s = A.s[slot];
+                s.x += Dbar / fmaxf(kEps, epsK);
+                s.y += pbar;
+                if (epsK > kEps) s.z += Dbar * (-rhoK / (epsK * epsK));
+                A.s[slot] = s;
+            }
         }
-        add3(A.x[slot], gx);
-        add3(A.v[slot], gv);
+        gx = groupSum3<G>(gx);
+        gv = groupSum3<G>(gv);
+        if (part == 0) {
+            add3(A.x[slot], gx);
+            add3(A.v[slot], gv);
+        }
     }
     const float2 t = blockSum2(gTan, gCap);
     if (threadIdx.x == 0) {
@@ -703,10 +755,11 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjVoidSelf(const SceneDev* __res
 }
 
 // A4b: voidage / adhesion pair terms from both ends.
+template <int G>
 __global__ void __launch_bounds__(kSlotAlign) kAdjVoidPairs(const SceneDev* __restrict__ scenes,
                                                             const int* __restrict__ blockScene, AdjBuffers A,
                                                             PassBuffers b) {
-    SF_ADJ_PROLOGUE
+    SF_ADJ_PROLOGUE_G
     const float4 pk4 = b.pos4[slot];
     if (pk4.w == 0.f) return;
     const float3 xk = xyz(pk4);
@@ -718,7 +771,7 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjVoidPairs(const SceneDev* __re
         const float satK = b.aux4[slot].z;
         const float vk = mk / rhoK;
         float gsat = 0.f;
-        LabelCursor<false> wc(S, b.lists, slot, xk, b.pos4);
+        LabelCursor<false, G> wc(S, b.lists, slot, xk, b.pos4, part);
         for (int j; wc.next(j);) {
             const float4 pj4 = b.pos4[j];
             const float3 d = xyz(pj4) - xk;  // x_j - x_k
@@ -737,13 +790,14 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjVoidPairs(const SceneDev* __re
             }
             gx -= (rj.w * vk) * gW;
         }
-        A.s[slot].w += gsat;
+        gsat = groupSum<G>(gsat);
+        if (part == 0) A.s[slot].w += gsat;
     } else {
         const float mk = pk4.w;
         const float4 rk = A.r[slot];
         const float epsfK = b.aux4[slot].y;
         float grho = 0.f, geps = 0.f;
-        LabelCursor<true> sc(S, b.lists, slot, xk, b.pos4);
+        LabelCursor<true, G> sc(S, b.lists, slot, xk, b.pos4, part);
         for (int j; sc.next(j);) {
             const float4 pj4 = b.pos4[j];
             const float3 d = xk - xyz(pj4);
@@ -765,12 +819,17 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjVoidPairs(const SceneDev* __re
             geps += rj.x * Vk * W;
             grho += s * (-mk / (rhoK * rhoK)) * W;
         }
-        float4 s = A.s[slot];
-        s.x += grho;
-        s.z += geps;
-        A.s[slot] = s;
+        grho = groupSum<G>(grho);
+        geps = groupSum<G>(geps);
+        if (part == 0) {
+            float4 s = A.s[slot];
+            s.x += grho;
+            s.z += geps;
+            A.s[slot] = s;
+        }
     }
-    add3(A.x[slot], gx);
+    gx = groupSum3<G>(gx);
+    if (part == 0) add3(A.x[slot], gx);
 }
 
 // A5a: sand: average flow = num / sat, sat = sum V_j W -> (num-bar, sat-bar total).
@@ -790,10 +849,11 @@ __global__ void kAdjFlowSelf(AdjBuffers A, PassBuffers b) {
 }
 
 // A5b: average flow / saturation / fluid voidage pair terms from both ends.
+template <int G>
 __global__ void __launch_bounds__(kSlotAlign) kAdjFlowPairs(const SceneDev* __restrict__ scenes,
                                                             const int* __restrict__ blockScene, AdjBuffers A,
                                                             PassBuffers b) {
-    SF_ADJ_PROLOGUE
+    SF_ADJ_PROLOGUE_G
     const float4 pk4 = b.pos4[slot];
     if (pk4.w == 0.f) return;
     const float3 xk = xyz(pk4);
@@ -801,7 +861,7 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjFlowPairs(const SceneDev* __re
     if (pk4.w < 0.f) {
         const float4 rk = A.r[slot];
         const float vk = -pk4.w / b.vel4[slot].w;
-        LabelCursor<false> wc(S, b.lists, slot, xk, b.pos4);
+        LabelCursor<false, G> wc(S, b.lists, slot, xk, b.pos4, part);
         for (int j; wc.next(j);) {
             const float4 pj4 = b.pos4[j];
             const float4 vj4 = b.vel4[j];
@@ -817,7 +877,7 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjFlowPairs(const SceneDev* __re
         const float rhoK = b.vel4[slot].w;
         const float Vk = mk / rhoK;
         float grho = 0.f;
-        LabelCursor<true> sc(S, b.lists, slot, xk, b.pos4);
+        LabelCursor<true, G> sc(S, b.lists, slot, xk, b.pos4, part);
         for (int j; sc.next(j);) {
             const float4 pj4 = b.pos4[j];
             const float3 d = xk - xyz(pj4);
@@ -831,8 +891,12 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjFlowPairs(const SceneDev* __re
             grho += s * (-mk / (rhoK * rhoK)) * W;
             gv += (Vk * W) * xyz(rj);
         }
-        A.s[slot].x += grho;
+        grho = groupSum<G>(grho);
+        if (part == 0) A.s[slot].x += grho;
     }
+    gx = groupSum3<G>(gx);
+    gv = groupSum3<G>(gv);
+    if (part != 0) return;
     add3(A.x[slot], gx);
     add3(A.v[slot], gv);
 }
@@ -858,28 +922,30 @@ __global__ void kAdjDensitySelf(const SceneDev* __restrict__ scenes, const int* 
 
 // A6b: density pair terms: own m_j W(x_k - x_j) and water j's m_k W(x_j - x_k),
 // boundary terms rho0 V_b W(x_k - x_b).
+template <int G>
 __global__ void __launch_bounds__(kSlotAlign) kAdjDensityPairs(const SceneDev* __restrict__ scenes,
                                                                const int* __restrict__ blockScene, AdjBuffers A,
                                                                PassBuffers b) {
-    SF_ADJ_PROLOGUE
+    SF_ADJ_PROLOGUE_G
     const float4 pk4 = b.pos4[slot];
     if (!(pk4.w > 0.f)) return;
     const float3 xk = xyz(pk4);
     const float mk = pk4.w;
     const float rk = A.r[slot].x;
     float3 gx = mk3(0.f, 0.f, 0.f);
-    LabelCursor<false> wc(S, b.lists, slot, xk, b.pos4);
+    LabelCursor<false, G> wc(S, b.lists, slot, xk, b.pos4, part);
     for (int j; wc.next(j);) {
         if (j == slot) continue;
         const float4 pj4 = b.pos4[j];
         gx += (rk * pj4.w + A.r[j].x * mk) * poly6Grad(S, xk - xyz(pj4));
     }
-    BoundaryCursor bc(S, b.lists, slot, xk, b.bpos4);
+    BoundaryCursor<G> bc(S, b.lists, slot, xk, b.bpos4, part);
     for (int bb; bc.next(bb);) {
         const float4 bj = b.bpos4[bb];
         gx += (rk * S.rho0 * fabsf(bj.w)) * poly6Grad(S, xk - xyz(bj));
     }
-    add3(A.x[slot], gx);
+    gx = groupSum3<G>(gx);
+    if (part == 0) add3(A.x[slot], gx);
 }
 
 // Cotangents of the substep's input positions and velocities, by id.
@@ -914,20 +980,49 @@ void launchAdjSeed(const LaunchCtx& c, const float4* pos4, const int* pid, const
                                                         lossPartial);
 }
 
+template <int G>
+void launchAdjPairs(const LaunchCtx& c, const AdjBuffers& A, const PassBuffers& b, float* paramPartial, int level) {
+    const dim3 g(c.slotBlocks * G), t(kSlotAlign);
+    const cudaStream_t s = c.stream;
+    switch (level) {
+    case 0: kAdjWater<G><<<g, t, 0, s>>>(c.scenes, c.blockScene, A, b); break;
+    case 1: kAdjSandPairs<G><<<g, t, 0, s>>>(c.scenes, c.blockScene, A, b, paramPartial); break;
+    case 2: kAdjVoidPairs<G><<<g, t, 0, s>>>(c.scenes, c.blockScene, A, b); break;
+    case 3: kAdjFlowPairs<G><<<g, t, 0, s>>>(c.scenes, c.blockScene, A, b); break;
+    default: kAdjDensityPairs<G><<<g, t, 0, s>>>(c.scenes, c.blockScene, A, b); break;
+    }
+}
+
+void launchPairs(const LaunchCtx& c, const AdjBuffers& A, const PassBuffers& b, float* paramPartial, int lanes,
+                 int level) {
+    switch (lanes) {
+    case 2: launchAdjPairs<2>(c, A, b, paramPartial, level); break;
+    case 4: launchAdjPairs<4>(c, A, b, paramPartial, level); break;
+    case 8: launchAdjPairs<8>(c, A, b, paramPartial, level); break;
+    default: launchAdjPairs<1>(c, A, b, paramPartial, level); break;
+    }
+}
+
+int adjointLanes(long long totalSlots, int smCount) {
+    int g = 1;
+    while (g < 8 && totalSlots * g < 2048LL * smCount) g *= 2;
+    return g;
+}
+
 int launchAdjSubstep(const LaunchCtx& c, const AdjBuffers& A, const PassBuffers& b, const int* pid, float dt,
-                     float* paramPartial) {
+                     float* paramPartial, int lanes) {
     const dim3 g(c.slotBlocks), t(kSlotAlign);
     const cudaStream_t s = c.stream;
     kAdjIntegrate<<<g, t, 0, s>>>(c.scenes, c.blockScene, A, b, pid, dt);
-    kAdjWater<<<g, t, 0, s>>>(c.scenes, c.blockScene, A, b);
-    kAdjSandSelf<<<g, t, 0, s>>>(c.scenes, c.blockScene, A, b, paramPartial);
-    kAdjSandPairs<<<g, t, 0, s>>>(c.scenes, c.blockScene, A, b, paramPartial);
+    launchPairs(c, A, b, paramPartial, lanes, 0);
+    kAdjSandSelf<<<g, t, 0, s>>>(c.scenes, c.blockScene, A, b, paramPartial, lanes);
+    launchPairs(c, A, b, paramPartial, lanes, 1);
     kAdjVoidSelf<<<g, t, 0, s>>>(c.scenes, c.blockScene, A, b);
-    kAdjVoidPairs<<<g, t, 0, s>>>(c.scenes, c.blockScene, A, b);
+    launchPairs(c, A, b, paramPartial, lanes, 2);
     kAdjFlowSelf<<<g, t, 0, s>>>(A, b);
-    kAdjFlowPairs<<<g, t, 0, s>>>(c.scenes, c.blockScene, A, b);
+    launchPairs(c, A, b, paramPartial, lanes, 3);
     kAdjDensitySelf<<<g, t, 0, s>>>(c.scenes, c.blockScene, A, b);
-    kAdjDensityPairs<<<g, t, 0, s>>>(c.scenes, c.blockScene, A, b);
+    launchPairs(c, A, b, paramPartial, lanes, 4);
     kAdjFinish<<<g, t, 0, s>>>(c.scenes, c.blockScene, A, b.pos4, pid);
     return 11;
 }

@@ -215,7 +215,8 @@ struct sf_handle {
     // reverse-mode buffers, allocated by the first sf_adjoint_run
     AdjBuffers adj{};
     float* adjTarget = nullptr;   // 3 floats per slot, indexed by slot_off + id
-    float* adjParam = nullptr;    // 3 per slot block
+    float* adjParam = nullptr;    // 3 per block of the adjoint pair kernels (adjLanes per slot block)
+    int adjLanes = 1;             // threads per slot of the adjoint pair kernels
     float2* adjLoss = nullptr;    // 1 per slot block
     char* snap = nullptr;         // state snapshots for checkpointing
     size_t snapBytes = 0;
@@ -232,6 +233,7 @@ struct sf_handle {
         err = std::string(what) + ": " + cudaGetErrorString(e);
         return SF_ERR_CUDA;
     }
+    int adjBlocks() const { return slotBlocks * adjLanes; }
     LaunchCtx ctx() const {
         LaunchCtx c;
         c.stream = stream;
@@ -1430,6 +1432,11 @@ sf_status growBuffer(sf_handle* h, char*& p, size_t& have, size_t need, const ch
 sf_status ensureAdjoint(sf_handle* h, size_t snapshots, size_t slabs) {
     const size_t M = size_t(h->totalSlots);
     if (!h->adj.adjX) {
+        int dev = 0, sms = 0;
+        if (h->cuda(cudaGetDevice(&dev), "cudaGetDevice") ||
+            h->cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"))
+            return SF_ERR_CUDA;
+        h->adjLanes = adjointLanes(h->totalSlots, sms);
         for (float4** p : {&h->adj.adjX, &h->adj.adjV, &h->adj.x, &h->adj.v, &h->adj.acc, &h->adj.flow, &h->adj.adh,
                            &h->adj.avgadh, &h->adj.drag, &h->adj.f, &h->adj.r, &h->adj.s}) {
             if (h->cuda(cudaMalloc(reinterpret_cast<void**>(p), sizeof(float4) * M), "cudaMalloc adjoint") ||
@@ -1437,7 +1444,7 @@ sf_status ensureAdjoint(sf_handle* h, size_t snapshots, size_t slabs) {
                 return SF_ERR_CUDA;
         }
         if (h->cuda(cudaMalloc(reinterpret_cast<void**>(&h->adjTarget), sizeof(float) * 3 * M), "cudaMalloc target") ||
-            h->cuda(cudaMalloc(reinterpret_cast<void**>(&h->adjParam), sizeof(float) * 3 * size_t(h->slotBlocks)),
+            h->cuda(cudaMalloc(reinterpret_cast<void**>(&h->adjParam), sizeof(float) * 3 * size_t(h->adjBlocks())),
                     "cudaMalloc param partials") ||
             h->cuda(cudaMalloc(reinterpret_cast<void**>(&h->adjLoss), sizeof(float2) * size_t(h->slotBlocks)),
                     "cudaMalloc loss partials") ||
@@ -1505,7 +1512,7 @@ sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t che
     launchAdjSeed(h->ctx(), h->pos[h->cur], h->pid[h->cur], h->adjTarget, h->adj.adjX, h->adj.adjV, h->adjLoss);
     h->launches += 1;
     if ((st = snapCopy(h, finalSnap, true))) return st;
-    if (h->cuda(cudaMemsetAsync(h->adjParam, 0, sizeof(float) * 3 * size_t(h->slotBlocks), h->stream),
+    if (h->cuda(cudaMemsetAsync(h->adjParam, 0, sizeof(float) * 3 * size_t(h->adjBlocks()), h->stream),
                 "clear parameter partials"))
         return SF_ERR_CUDA;
     cudaEventRecord(ev[1], h->stream);
@@ -1521,7 +1528,7 @@ sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t che
         }
         for (int64_t t = len - 1; t >= 0; --t) {
             const AdjSlab sl = slab(t);
-            h->launches += launchAdjSubstep(h->ctx(), h->adj, slabBuffers(h, sl), sl.pid, dt, h->adjParam);
+            h->launches += launchAdjSubstep(h->ctx(), h->adj, slabBuffers(h, sl), sl.pid, dt, h->adjParam, h->adjLanes);
             if (h->cuda(cudaGetLastError(), "adjoint launch")) return SF_ERR_CUDA;
         }
     }
@@ -1530,7 +1537,7 @@ sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t che
 
     // per-scene reductions in block order, and the id-ordered gradients
     std::vector<float2> lossPart(size_t(h->slotBlocks));
-    std::vector<float> paramPart(3 * size_t(h->slotBlocks));
+    std::vector<float> paramPart(3 * size_t(h->adjBlocks()));
     std::vector<float4> gx, gv;
     if (h->cuda(cudaMemcpyAsync(lossPart.data(), h->adjLoss, sizeof(float2) * lossPart.size(), cudaMemcpyDeviceToHost,
                                 h->stream),
@@ -1547,8 +1554,9 @@ sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t che
         for (int b = S.slot_off / kSlotAlign; b < (S.slot_off + S.slot_cap) / kSlotAlign; ++b) {
             l += lossPart[size_t(b)].x;
             ns += lossPart[size_t(b)].y;
-            for (int k = 0; k < 3; ++k) g[k] += paramPart[3 * size_t(b) + size_t(k)];
         }
+        for (int b = S.slot_off / kSlotAlign * h->adjLanes; b < (S.slot_off + S.slot_cap) / kSlotAlign * h->adjLanes; ++b)
+            for (int k = 0; k < 3; ++k) g[k] += paramPart[3 * size_t(b) + size_t(k)];
         const double inv = ns > 0.0 ? 1.0 / ns : 0.0;
         loss_out[s] = float(l * inv);
         if (grad_params_out)
