@@ -57,20 +57,6 @@ namespace sfg {
     const int sid = blockScene[(blockIdx.x * (blockDim.x / G)) / kSlotAlign]; \
     const SceneDev& S = scenes[sid];
 
-// Sum over the G lanes of a slot (G divides 32; all G lanes call it).
-template <int G> __device__ __forceinline__ float groupSum(float v) {
-    if (G > 1) {
-        const unsigned lane = threadIdx.x & 31u;
-        const unsigned mask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << (lane & ~unsigned(G - 1));
-#pragma unroll
-        for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
-    }
-    return v;
-}
-template <int G> __device__ __forceinline__ float3 groupSum3(float3 v) {
-    return make_float3(groupSum<G>(v.x), groupSum<G>(v.y), groupSum<G>(v.z));
-}
-
 // ------------------------------------------------------ neighbour cursors
 // The neighbours of one label (list, or the stencil when the list
 // overflowed) from a single call site, so that the loop body is inlined.
@@ -1001,12 +987,6 @@ void launchPairs(const LaunchCtx& c, const AdjBuffers& A, const PassBuffers& b, 
     case 8: launchAdjPairs<8>(c, A, b, paramPartial, level); break;
     default: launchAdjPairs<1>(c, A, b, paramPartial, level); break;
     }
-}
-
-int adjointLanes(long long totalSlots, int smCount) {
-    int g = 1;
-    while (g < 8 && totalSlots * g < 2048LL * smCount) g *= 2;
-    return g;
 }
 
 int launchAdjSubstep(const LaunchCtx& c, const AdjBuffers& A, const PassBuffers& b, const int* pid, float dt,

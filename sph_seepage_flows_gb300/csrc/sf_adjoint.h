@@ -51,13 +51,10 @@ void launchAdjSeed(const LaunchCtx& c, const float4* pos4, const int* pid, const
 // of that substep were recomputed into b. Adds the block partials of the
 // parameter cotangents (tan friction angle, capillary scale, permeability
 // scale) into paramPartial[3 * block + k]. Returns kernels launched.
-// lanes: threads per slot of the pair kernels (1, 2, 4 or 8; adjointLanes);
+// lanes: threads per slot of the pair kernels (1, 2, 4 or 8; lanesForSlots);
 // paramPartial holds 3 floats per block of the pair kernels, i.e. lanes
 // blocks per kSlotAlign slots.
 int launchAdjSubstep(const LaunchCtx& c, const AdjBuffers& A, const PassBuffers& b, const int* pid, float dt,
                      float* paramPartial, int lanes);
-// Threads per slot of the pair kernels for totalSlots slots on a GPU with
-// smCount SMs: doubled (up to 8) while fewer than 2048 threads per SM would run.
-int adjointLanes(long long totalSlots, int smCount);
 
 }  // namespace sfg

@@ -211,12 +211,12 @@ struct sf_handle {
     GraphCache graph1[2];  // one-substep graphs, by starting buffer set
     int nbrCap = kMinNbr;                 // particle neighbour list capacity (per slot)
     int block[kTunedPasses] = {kSlotAlign, kSlotAlign, kSlotAlign, kSlotAlign, kSlotAlign, kSlotAlign};
+    int lanes = 1;  // threads per slot of the momentum passes and the adjoint pair kernels
     unsigned int* dProbe = nullptr;       // neighbour-count probe word
     // reverse-mode buffers, allocated by the first sf_adjoint_run
     AdjBuffers adj{};
     float* adjTarget = nullptr;   // 3 floats per slot, indexed by slot_off + id
-    float* adjParam = nullptr;    // 3 per block of the adjoint pair kernels (adjLanes per slot block)
-    int adjLanes = 1;             // threads per slot of the adjoint pair kernels
+    float* adjParam = nullptr;    // 3 per block of the adjoint pair kernels (lanes per slot block)
     float2* adjLoss = nullptr;    // 1 per slot block
     char* snap = nullptr;         // state snapshots for checkpointing
     size_t snapBytes = 0;
@@ -233,7 +233,7 @@ struct sf_handle {
         err = std::string(what) + ": " + cudaGetErrorString(e);
         return SF_ERR_CUDA;
     }
-    int adjBlocks() const { return slotBlocks * adjLanes; }
+    int adjBlocks() const { return slotBlocks * lanes; }
     LaunchCtx ctx() const {
         LaunchCtx c;
         c.stream = stream;
@@ -243,6 +243,7 @@ struct sf_handle {
         c.errWord = dErr;
         c.slotBlocks = slotBlocks;
         for (int k = 0; k < kTunedPasses; ++k) c.block[k] = block[k];
+        c.lanes = lanes;
         return c;
     }
     PassBuffers buffers() const {
@@ -672,6 +673,13 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
     }
     if (h->cuda(cudaGetLastError(), "boundary volume") || h->cuda(cudaStreamSynchronize(h->stream), "create sync"))
         return bail(SF_ERR_CUDA);
+    {
+        int dev = 0, sms = 0;
+        if (h->cuda(cudaGetDevice(&dev), "cudaGetDevice") ||
+            h->cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"))
+            return bail(SF_ERR_CUDA);
+        h->lanes = lanesForSlots(h->totalSlots, sms);
+    }
     // neighbour list capacity from the initial neighbour counts
     if (probeListCapacity(h) != SF_OK) return bail(SF_ERR_CUDA);
     *out = h;
@@ -1432,11 +1440,6 @@ sf_status growBuffer(sf_handle* h, char*& p, size_t& have, size_t need, const ch
 sf_status ensureAdjoint(sf_handle* h, size_t snapshots, size_t slabs) {
     const size_t M = size_t(h->totalSlots);
     if (!h->adj.adjX) {
-        int dev = 0, sms = 0;
-        if (h->cuda(cudaGetDevice(&dev), "cudaGetDevice") ||
-            h->cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"))
-            return SF_ERR_CUDA;
-        h->adjLanes = adjointLanes(h->totalSlots, sms);
         for (float4** p : {&h->adj.adjX, &h->adj.adjV, &h->adj.x, &h->adj.v, &h->adj.acc, &h->adj.flow, &h->adj.adh,
                            &h->adj.avgadh, &h->adj.drag, &h->adj.f, &h->adj.r, &h->adj.s}) {
             if (h->cuda(cudaMalloc(reinterpret_cast<void**>(p), sizeof(float4) * M), "cudaMalloc adjoint") ||
@@ -1528,7 +1531,7 @@ sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t che
         }
         for (int64_t t = len - 1; t >= 0; --t) {
             const AdjSlab sl = slab(t);
-            h->launches += launchAdjSubstep(h->ctx(), h->adj, slabBuffers(h, sl), sl.pid, dt, h->adjParam, h->adjLanes);
+            h->launches += launchAdjSubstep(h->ctx(), h->adj, slabBuffers(h, sl), sl.pid, dt, h->adjParam, h->lanes);
             if (h->cuda(cudaGetLastError(), "adjoint launch")) return SF_ERR_CUDA;
         }
     }
@@ -1555,7 +1558,7 @@ sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t che
             l += lossPart[size_t(b)].x;
             ns += lossPart[size_t(b)].y;
         }
-        for (int b = S.slot_off / kSlotAlign * h->adjLanes; b < (S.slot_off + S.slot_cap) / kSlotAlign * h->adjLanes; ++b)
+        for (int b = S.slot_off / kSlotAlign * h->lanes; b < (S.slot_off + S.slot_cap) / kSlotAlign * h->lanes; ++b)
             for (int k = 0; k < 3; ++k) g[k] += paramPart[3 * size_t(b) + size_t(k)];
         const double inv = ns > 0.0 ? 1.0 / ns : 0.0;
         loss_out[s] = float(l * inv);

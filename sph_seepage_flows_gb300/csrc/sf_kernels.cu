@@ -39,6 +39,17 @@ namespace sfg {
     const int sid = blockScene[(blockIdx.x * blockDim.x) / kSlotAlign];    \
     const SceneDev& S = scenes[sid];
 
+// The momentum passes run G consecutive threads per slot (G = 1, 2, 4 or 8,
+// chosen per handle by the slot count): lane `part` takes every G-th
+// neighbour and lane 0 adds up the lanes' sums and writes the slot. Their
+// sums are already in a different order from the reference's, so the split
+// only moves FP32 rounding; small scenes get G times the threads in flight.
+#define SF_SLOT_PROLOGUE_G                                                      \
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;                      \
+    const int slot = gid / G, part = gid % G;                                   \
+    const int sid = blockScene[(blockIdx.x * (blockDim.x / G)) / kSlotAlign];   \
+    const SceneDev& S = scenes[sid];
+
 // ---------------------------------------------------------------------- keys
 // Pos2GridHash (helper_thrust.cuh:66-89) into the global cell space; parking
 // slots get the scene's parking cell.
@@ -429,16 +440,17 @@ __global__ void __launch_bounds__(kSlotAlign) kVoidageAdhesion(
 // adhesion terms of water neighbours (240-273, 314-341), DEM against shape
 // boundary particles (52-81) and ComputeDemWorldBoundaryForces
 // (cuda_dem_solver_common_gpu.cuh:132-199). acc = g + 2 (f + df) / m.
+template <int G>
 __global__ void __launch_bounds__(kSlotAlign, 5) kSandMomentum(
     const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene, NbrLists L,
     const float4* __restrict__ pos4, const float4* __restrict__ vel4, const float4* __restrict__ aux4,
     const float4* __restrict__ flow4, const float4* __restrict__ avgadh4, const float4* __restrict__ mat4,
     const float4* __restrict__ bpos4, float2* __restrict__ dp, float4* __restrict__ drag4,
     float4* __restrict__ acc4) {
-    SF_SLOT_PROLOGUE
+    SF_SLOT_PROLOGUE_G
     const float4 pi4 = pos4[slot];
     if (!(pi4.w < 0.f)) {
-        if (pi4.w > 0.f) drag4[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (pi4.w > 0.f && part == 0) drag4[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
     const float3 pi = xyz(pi4);
@@ -461,15 +473,15 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kSandMomentum(
     if (cc <= kMaxContact) {
         const unsigned* __restrict__ p = L.cnbr + slot;
 #pragma unroll 2
-        for (int k = 0; k < cc; ++k) contact(int(p[k * L.M]));
+        for (int k = part; k < cc; k += G) contact(int(p[k * L.M]));
     } else {
-        forSandNeighbors(S, L, slot, pi, pos4, [&](int j) {
+        forSandNeighbors<G>(S, L, slot, pi, pos4, [&](int j) {
             if (j == slot) return;
             const float3 dij = xyz(pos4[j]) - pi;
             if (dot3(dij, dij) < S.dem_reach2) contact(j);
-        });
+        }, part);
     }
-    forWaterNeighbors(S, L, slot, pi, pos4, [&](int j) {
+    forWaterNeighbors<G>(S, L, slot, pi, pos4, [&](int j) {
         const float4 pj = pos4[j];
         const float3 dij = pi - xyz(pj);
         const float4 aj = aux4[j];
@@ -480,13 +492,16 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kSandMomentum(
             f += -mi * pj.w * aj.x / fmaxf(kEps, di * dj) * spikyGrad(S, dij);
         }
         f += wij * vol_i * xyz(avgadh4[j]);
-    });
+    }, part);
     if (S.shape_boundary) {
-        forBoundaryNeighbors(S, L, slot, pi, bpos4, [&](int b) {
+        forBoundaryNeighbors<G>(S, L, slot, pi, bpos4, [&](int b) {
             const float4 bj = bpos4[b];
             if (bj.w < 0.f) f += demForce(pi - xyz(bj), mk3(-vi.x, -vi.y, -vi.z), S.rij2, S.kn, S.ks, S.tan2);
-        });
+        }, part);
     }
+    f = groupSum3<G>(f);
+    v_w = groupSum<G>(v_w);
+    if (part != 0) return;
     // ComputeDemWorldBoundaryForces; the z-min wall tests 2 * rij (DEM:191)
     {
         const float rij = S.wall_rij;
@@ -521,12 +536,13 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kSandMomentum(
 // (cuda_sph_solver_common_gpu.cuh:89-139, called with rho0 as the particle
 // density). acc = g + (a - F_adh / m). Every thread then contributes |acc|
 // of its slot (sand included) to the scene maximum (cuda_wcsph_sf_solver.cu:43-47).
+template <int G>
 __global__ void __launch_bounds__(kSlotAlign, 5) kWaterMomentum(
     const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene, SceneState* __restrict__ state,
     NbrLists L, const float4* __restrict__ pos4, const float4* __restrict__ vel4, const float4* __restrict__ aux4,
     const float4* __restrict__ drag4, const float4* __restrict__ adh4, const float4* __restrict__ bpos4,
     const float2* __restrict__ dp, float4* __restrict__ acc4, unsigned int* errWord) {
-    SF_SLOT_PROLOGUE
+    SF_SLOT_PROLOGUE_G
     const float4 pi4 = pos4[slot];
     float alen = 0.f;
     if (pi4.w > 0.f) {
@@ -538,7 +554,7 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kWaterMomentum(
         const float pri = aux4[slot].x;
         const float pterm_i = dpi.y;
         float3 a = mk3(0.f, 0.f, 0.f);
-        forWaterNeighbors(S, L, slot, pi, pos4, [&](int j) {
+        forWaterNeighbors<G>(S, L, slot, pi, pos4, [&](int j) {
             if (j == slot) return;
             const float4 pj = pos4[j];
             const float3 dij = pi - xyz(pj);
@@ -552,8 +568,8 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kWaterMomentum(
                 const float pij = -S.nu / (di + dj) * (dd / (dot3(dij, dij) + kEps));
                 a += -pj.w * pij * nab;
             }
-        });
-        forSandNeighbors(S, L, slot, pi, pos4, [&](int j) {
+        }, part);
+        forSandNeighbors<G>(S, L, slot, pi, pos4, [&](int j) {
             const float4 pj = pos4[j];
             const float3 dij = pi - xyz(pj);
             const float dj = vel4[j].w;
@@ -562,10 +578,10 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kWaterMomentum(
             const float3 buoy = pj.w * pri / fmaxf(kEps, di * dj) * nab;  // -m_j with m_j = -w
             const float3 drag = -wij / di * xyz(drag4[j]);
             a += buoy + drag;
-        });
+        }, part);
         const float bp = pri / fmaxf(kEps, S.rho0 * S.rho0);
         const float bvis = -S.bnu / (2.f * S.rho0);
-        forBoundaryNeighbors(S, L, slot, pi, bpos4, [&](int b) {
+        forBoundaryNeighbors<G>(S, L, slot, pi, bpos4, [&](int b) {
             const float4 bj = bpos4[b];
             const float3 dij = pi - xyz(bj);
             const float3 nab = spikyGrad(S, dij);
@@ -575,12 +591,15 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kWaterMomentum(
                 const float pij = bvis * (dd / (dot3(dij, dij) + kEps));
                 a += -fabsf(bj.w) * S.rho0 * pij * nab;
             }
-        });
-        const float3 g = mk3(0.f, 0.f, 0.f) + mk3(S.gvx, S.gvy, S.gvz);
-        const float3 acc = g + (a - xyz(adh4[slot]) / pi4.w);
-        acc4[slot] = make_float4(acc.x, acc.y, acc.z, 0.f);
-        alen = len3(acc);
-    } else if (pi4.w < 0.f) {
+        }, part);
+        a = groupSum3<G>(a);
+        if (part == 0) {
+            const float3 g = mk3(0.f, 0.f, 0.f) + mk3(S.gvx, S.gvy, S.gvz);
+            const float3 acc = g + (a - xyz(adh4[slot]) / pi4.w);
+            acc4[slot] = make_float4(acc.x, acc.y, acc.z, 0.f);
+            alen = len3(acc);
+        }
+    } else if (pi4.w < 0.f && part == 0) {
         alen = len3(xyz(acc4[slot]));
     }
     if (!(alen <= 3.0e38f) && pi4.w != 0.f) atomicOr(errWord, 1u);
@@ -706,6 +725,12 @@ __global__ void kNeighborCountMax(const SceneDev* __restrict__ scenes, const int
 }
 
 // ------------------------------------------------------------ launchers
+int lanesForSlots(long long totalSlots, int smCount) {
+    int g = 1;
+    while (g < 8 && totalSlots * g < 2048LL * smCount) g *= 2;
+    return g;
+}
+
 // Blocks of a tuned pass over all slots.
 static inline int grid(const LaunchCtx& c, int pass) { return c.slotBlocks * (kSlotAlign / c.block[pass]); }
 
@@ -738,16 +763,32 @@ void launchVoidageAdhesion(const LaunchCtx& c, const PassBuffers& b) {
                                                                 b.aux4, b.adh4, b.avgadh4, b.col4, b.dp);
 }
 
+template <int G> void launchSandMomentumG(const LaunchCtx& c, const PassBuffers& b) {
+    kSandMomentum<G><<<grid(c, kPassSand) * G, c.block[kPassSand], 0, c.stream>>>(
+        c.scenes, c.blockScene, b.lists, b.pos4, b.vel4, b.aux4, b.flow4, b.avgadh4, b.mat4, b.bpos4, b.dp, b.drag4,
+        b.acc4);
+}
 void launchSandMomentum(const LaunchCtx& c, const PassBuffers& b) {
-    kSandMomentum<<<grid(c, kPassSand), c.block[kPassSand], 0, c.stream>>>(c.scenes, c.blockScene, b.lists, b.pos4, b.vel4,
-                                                             b.aux4, b.flow4, b.avgadh4, b.mat4, b.bpos4, b.dp,
-                                                             b.drag4, b.acc4);
+    switch (c.lanes) {
+    case 2: launchSandMomentumG<2>(c, b); break;
+    case 4: launchSandMomentumG<4>(c, b); break;
+    case 8: launchSandMomentumG<8>(c, b); break;
+    default: launchSandMomentumG<1>(c, b); break;
+    }
 }
 
+template <int G> void launchWaterMomentumG(const LaunchCtx& c, const PassBuffers& b) {
+    kWaterMomentum<G><<<grid(c, kPassWater) * G, c.block[kPassWater], 0, c.stream>>>(
+        c.scenes, c.blockScene, c.state, b.lists, b.pos4, b.vel4, b.aux4, b.drag4, b.adh4, b.bpos4, b.dp, b.acc4,
+        c.errWord);
+}
 void launchWaterMomentum(const LaunchCtx& c, const PassBuffers& b) {
-    kWaterMomentum<<<grid(c, kPassWater), c.block[kPassWater], 0, c.stream>>>(c.scenes, c.blockScene, c.state, b.lists, b.pos4,
-                                                              b.vel4, b.aux4, b.drag4, b.adh4, b.bpos4, b.dp,
-                                                              b.acc4, c.errWord);
+    switch (c.lanes) {
+    case 2: launchWaterMomentumG<2>(c, b); break;
+    case 4: launchWaterMomentumG<4>(c, b); break;
+    case 8: launchWaterMomentumG<8>(c, b); break;
+    default: launchWaterMomentumG<1>(c, b); break;
+    }
 }
 
 void launchIntegrate(const LaunchCtx& c, const PassBuffers& b, float timeArg, int adaptive) {

@@ -22,6 +22,7 @@ struct LaunchCtx {
     unsigned int* errWord;    // device error word
     int slotBlocks;           // total slots / kSlotAlign
     int block[kTunedPasses];  // threads per block of each tuned pass
+    int lanes;                // threads per slot of the momentum passes (1, 2, 4 or 8)
 };
 
 // Neighbour lists of the current substep (column-major: entry k of slot i at
@@ -87,6 +88,11 @@ struct PassBuffers {
     // of its average adhesion for the same reason.
     float2* dp;
 };
+
+// Threads per slot of the lane-split passes (momentum passes and the adjoint
+// pair kernels) for totalSlots slots on a GPU with smCount SMs: doubled, up
+// to 8, while fewer than 2048 threads per SM would run.
+int lanesForSlots(long long totalSlots, int smCount);
 
 void launchKeys(const LaunchCtx& c, const float4* pos4, unsigned int* keys);
 void launchBoundaryVolume(const LaunchCtx& c, int sid, int nb, float4* bpos4, const int* blabel,

@@ -34,10 +34,11 @@ __device__ __forceinline__ bool inReach(const SceneDev& S, float3 d) { return do
 
 // Neighbours of one label within reach of slot, in stencil order: the sand
 // part (kSand) or the water part of the list, or the stencil when the list
-// overflowed.
-template <bool kSand, typename F>
+// overflowed. With G lanes per slot, lane `part` gets every G-th of them
+// starting at the part-th (G = 1: all, in order).
+template <bool kSand, int G = 1, typename F>
 __device__ __forceinline__ void forLabelNeighbors(const SceneDev& S, const NbrLists& L, int slot, float3 pi,
-                                                  const float4* __restrict__ pos4, F&& f) {
+                                                  const float4* __restrict__ pos4, F&& f, int part = 0) {
     const unsigned c = L.cnt[slot];
     if (int(c & 0xFFFFu) + int(c >> 16) <= L.cap) {
         const int n = kSand ? int(c & 0xFFFFu) : int(c >> 16);
@@ -45,60 +46,80 @@ __device__ __forceinline__ void forLabelNeighbors(const SceneDev& S, const NbrLi
         const long long step = kSand ? L.M : -L.M;
         // indices are loaded a group ahead so the neighbour gathers of
         // consecutive entries overlap
-        int k = 0;
-        for (; k + 4 <= n; k += 4) {
-            const int j0 = int(p[k * step]), j1 = int(p[(k + 1) * step]);
-            const int j2 = int(p[(k + 2) * step]), j3 = int(p[(k + 3) * step]);
+        int k = part;
+        for (; k + 3 * G < n; k += 4 * G) {
+            const int j0 = int(p[k * step]), j1 = int(p[(k + G) * step]);
+            const int j2 = int(p[(k + 2 * G) * step]), j3 = int(p[(k + 3 * G) * step]);
             f(j0);
             f(j1);
             f(j2);
             f(j3);
         }
-        for (; k < n; ++k) f(int(p[k * step]));
+        for (; k < n; k += G) f(int(p[k * step]));
     } else {
         // stencil walk in the same order: 9 (dx, dy) columns, 3 contiguous z-cells each
         const int3 c = cellOf(S, pi);
         const int z0 = max(c.z - 1, 0), z1 = min(c.z + 1, S.gz - 1) + 1;
+        unsigned hits = 0;
         for (int x = max(c.x - 1, 0); x <= min(c.x + 1, S.gx - 1); ++x)
             for (int y = max(c.y - 1, 0); y <= min(c.y + 1, S.gy - 1); ++y) {
                 const int base = S.cell_off + (x * S.gy + y) * S.gz;
                 for (unsigned j = L.cs[base + z0]; j < L.cs[base + z1]; ++j) {
                     const float4 pj = pos4[j];
-                    if ((kSand ? pj.w < 0.f : pj.w > 0.f) && inReach(S, pi - xyz(pj))) f(int(j));
+                    if ((kSand ? pj.w < 0.f : pj.w > 0.f) && inReach(S, pi - xyz(pj)))
+                        if (G == 1 || int(hits++ % unsigned(G)) == part) f(int(j));
                 }
             }
     }
 }
-template <typename F>
+template <int G = 1, typename F>
 __device__ __forceinline__ void forSandNeighbors(const SceneDev& S, const NbrLists& L, int slot, float3 pi,
-                                                 const float4* __restrict__ pos4, F&& f) {
-    forLabelNeighbors<true>(S, L, slot, pi, pos4, f);
+                                                 const float4* __restrict__ pos4, F&& f, int part = 0) {
+    forLabelNeighbors<true, G>(S, L, slot, pi, pos4, f, part);
 }
-template <typename F>
+template <int G = 1, typename F>
 __device__ __forceinline__ void forWaterNeighbors(const SceneDev& S, const NbrLists& L, int slot, float3 pi,
-                                                  const float4* __restrict__ pos4, F&& f) {
-    forLabelNeighbors<false>(S, L, slot, pi, pos4, f);
+                                                  const float4* __restrict__ pos4, F&& f, int part = 0) {
+    forLabelNeighbors<false, G>(S, L, slot, pi, pos4, f, part);
 }
 
-// Boundary particles within reach of slot, in stencil order.
-template <typename F>
+// Boundary particles within reach of slot, in stencil order (lane-strided
+// like forLabelNeighbors).
+template <int G = 1, typename F>
 __device__ __forceinline__ void forBoundaryNeighbors(const SceneDev& S, const NbrLists& L, int slot, float3 pi,
-                                                     const float4* __restrict__ bpos4, F&& f) {
+                                                     const float4* __restrict__ bpos4, F&& f, int part = 0) {
     const int c = L.bcnt[slot];
     if (c <= kMaxBNbr) {
         const unsigned* __restrict__ p = L.bnbr + slot;
 #pragma unroll 1
-        for (int k = 0; k < c; ++k) f(int(p[size_t(k) * L.M]));
+        for (int k = part; k < c; k += G) f(int(p[size_t(k) * L.M]));
     } else {
         const int3 c = cellOf(S, pi);
         const int z0 = max(c.z - 1, 0), z1 = min(c.z + 1, S.gz - 1) + 1;
+        unsigned hits = 0;
         for (int x = max(c.x - 1, 0); x <= min(c.x + 1, S.gx - 1); ++x)
             for (int y = max(c.y - 1, 0); y <= min(c.y + 1, S.gy - 1); ++y) {
                 const int base = S.cell_off + (x * S.gy + y) * S.gz;
                 for (unsigned j = L.bcs[base + z0]; j < L.bcs[base + z1]; ++j)
-                    if (inReach(S, pi - xyz(bpos4[j]))) f(int(j));
+                    if (inReach(S, pi - xyz(bpos4[j])))
+                        if (G == 1 || int(hits++ % unsigned(G)) == part) f(int(j));
             }
     }
+}
+
+// Sum over the G lanes of a slot (G consecutive lanes of one warp, G divides
+// 32; all G lanes call it).
+template <int G> __device__ __forceinline__ float groupSum(float v) {
+    if (G > 1) {
+        const unsigned lane = threadIdx.x & 31u;
+        const unsigned mask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << (lane & ~unsigned(G - 1));
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+    }
+    return v;
+}
+template <int G> __device__ __forceinline__ float3 groupSum3(float3 v) {
+    return make_float3(groupSum<G>(v.x), groupSum<G>(v.y), groupSum<G>(v.z));
 }
 
 }  // namespace sfg
