@@ -317,12 +317,16 @@ __global__ void __launch_bounds__(kSlotAlign, 6) kDensity(const SceneDev* __rest
 // ComputeSFAvgFlow_CUDA with ComputeSFSandVolume and ComputeSFAvgFlow
 // (cuda_sph_sf_solver_gpu.cuh:111-173, 510-572). The two sub-loops feed
 // disjoint accumulators, so one sweep keeps every sum's reference order.
+// Small scenes run G lanes per slot: the lanes share the term evaluations
+// and fold the terms in list order (forLabelNeighborsOrdered), so the sums
+// stay bit-identical.
+template <int G>
 __global__ void __launch_bounds__(kSlotAlign) kAvgFlow(const SceneDev* __restrict__ scenes,
                                                        const int* __restrict__ blockScene, NbrLists L,
                                                        const float4* __restrict__ pos4,
                                                        const float4* __restrict__ vel4, float4* __restrict__ aux4,
                                                        float4* __restrict__ flow4) {
-    SF_SLOT_PROLOGUE
+    SF_SLOT_PROLOGUE_G
     const float4 pi4 = pos4[slot];
     if (pi4.w == 0.f) return;
     const float3 pi = xyz(pi4);
@@ -330,29 +334,57 @@ __global__ void __launch_bounds__(kSlotAlign) kAvgFlow(const SceneDev* __restric
     float v_s = 0.f, v_w = 0.f, sand_volume = 0.f;
     float3 avg_s = mk3(0.f, 0.f, 0.f), avg_w = avg_s;
     // sand neighbours: sand volume (every i) and, for water i, the sand average flow
-    forSandNeighbors(S, L, slot, pi, pos4, [&](int j) {
-        const float4 pj = pos4[j];
-        const float4 vj4 = vel4[j];
-        const float mj = -pj.w;
-        const float wij = poly6(S, len3(pi - xyz(pj)));
-        if (vj4.w != 0.f) sand_volume += mj / vj4.w * wij;
-        if (!sandI) {
-            const float vj = mj / vj4.w;
-            avg_w += xyz(vj4) * vj * wij;
-            v_w += vj * wij;
-        }
-    });
-    // water neighbours of sand i: the water average flow and the saturation
-    if (sandI) {
-        forWaterNeighbors(S, L, slot, pi, pos4, [&](int j) {
+    forLabelNeighborsOrdered<true, G, 6>(
+        S, L, slot, pi, pos4, part,
+        [&](int j) {
             const float4 pj = pos4[j];
             const float4 vj4 = vel4[j];
-            const float vj = pj.w / vj4.w;
+            const float mj = -pj.w;
             const float wij = poly6(S, len3(pi - xyz(pj)));
-            avg_s += xyz(vj4) * vj * wij;
-            v_s += vj * wij;
+            Terms<6> t;
+            t.v[0] = vj4.w != 0.f ? mj / vj4.w * wij : 0.f;
+            t.v[1] = vj4.w != 0.f ? 1.f : 0.f;
+            t.v[2] = t.v[3] = t.v[4] = t.v[5] = 0.f;
+            if (!sandI) {
+                const float vj = mj / vj4.w;
+                const float3 a = xyz(vj4) * vj * wij;
+                t.v[2] = a.x;
+                t.v[3] = a.y;
+                t.v[4] = a.z;
+                t.v[5] = vj * wij;
+            }
+            return t;
+        },
+        [&](const Terms<6>& t) {
+            if (t.v[1] != 0.f) sand_volume += t.v[0];
+            if (!sandI) {
+                avg_w += mk3(t.v[2], t.v[3], t.v[4]);
+                v_w += t.v[5];
+            }
         });
+    // water neighbours of sand i: the water average flow and the saturation
+    if (sandI) {
+        forLabelNeighborsOrdered<false, G, 4>(
+            S, L, slot, pi, pos4, part,
+            [&](int j) {
+                const float4 pj = pos4[j];
+                const float4 vj4 = vel4[j];
+                const float vj = pj.w / vj4.w;
+                const float wij = poly6(S, len3(pi - xyz(pj)));
+                const float3 a = xyz(vj4) * vj * wij;
+                Terms<4> t;
+                t.v[0] = a.x;
+                t.v[1] = a.y;
+                t.v[2] = a.z;
+                t.v[3] = vj * wij;
+                return t;
+            },
+            [&](const Terms<4>& t) {
+                avg_s += mk3(t.v[0], t.v[1], t.v[2]);
+                v_s += t.v[3];
+            });
     }
+    if (part != 0) return;
     float3 avg;
     if (!sandI && v_w != 0.f)
         avg = avg_w / v_w;
@@ -373,25 +405,36 @@ __global__ void __launch_bounds__(kSlotAlign) kAvgFlow(const SceneDev* __restric
 // 680-721) and ComputeSFWetSandColor_CUDA (952-977). Water: the SF or MULTI
 // water adhesion kernel (175-207, 574-678). Reads the fluid voidage (aux.y)
 // of water neighbours and writes the final voidage (aux.w) of sand slots.
+// Lane-split like kAvgFlow (order-preserving sums).
+template <int G>
 __global__ void __launch_bounds__(kSlotAlign) kVoidageAdhesion(
     const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene, NbrLists L,
     const float4* __restrict__ pos4, const float4* __restrict__ vel4, float4* __restrict__ aux4,
     float4* __restrict__ adh4, float4* __restrict__ avgadh4, float4* __restrict__ col4, float2* __restrict__ dp) {
-    SF_SLOT_PROLOGUE
+    SF_SLOT_PROLOGUE_G
     const float4 pi4 = pos4[slot];
     if (pi4.w == 0.f) return;
     const float3 pi = xyz(pi4);
     if (pi4.w < 0.f) {
         const float sat = aux4[slot].z;
         float num = 0.f, den = 0.f;
-        forWaterNeighbors(S, L, slot, pi, pos4, [&](int j) {
-            const float4 pj = pos4[j];
-            const float3 dij = pi - xyz(pj);
-            const float vj = pj.w / vel4[j].w;
-            const float wij = poly6(S, len3(dij));
-            num += aux4[j].y * vj * wij;
-            den += vj * wij;
-        });
+        forLabelNeighborsOrdered<false, G, 2>(
+            S, L, slot, pi, pos4, part,
+            [&](int j) {
+                const float4 pj = pos4[j];
+                const float3 dij = pi - xyz(pj);
+                const float vj = pj.w / vel4[j].w;
+                const float wij = poly6(S, len3(dij));
+                Terms<2> t;
+                t.v[0] = aux4[j].y * vj * wij;
+                t.v[1] = vj * wij;
+                return t;
+            },
+            [&](const Terms<2>& t) {
+                num += t.v[0];
+                den += t.v[1];
+            });
+        if (part != 0) return;
         aux4[slot].w = den != 0.f ? num / den : 0.f;
         dp[slot] = make_float2(den, 0.f);  // the quotient's denominator, for the adjoint
         // wet-sand colour ratchet
@@ -409,17 +452,29 @@ __global__ void __launch_bounds__(kSlotAlign) kVoidageAdhesion(
         const float mi = pi4.w;
         float v_s = 0.f;
         float3 ad = mk3(0.f, 0.f, 0.f);
-        forSandNeighbors(S, L, slot, pi, pos4, [&](int j) {
-            const float4 pj = pos4[j];
-            const float3 dpij = pi - xyz(pj);
-            const float ldp = len3(dpij);
-            const float wij = poly6(S, ldp);
-            const float adij = adhesionSpline(S, ldp);
-            const float mj = -pj.w;
-            ad += bezier(S.adhG, aux4[j].z) * mi * mj * adij * dpij / fmaxf(kEps, ldp);
-            const float vj = mj / vel4[j].w;
-            v_s += vj * wij;
-        });
+        forLabelNeighborsOrdered<true, G, 4>(
+            S, L, slot, pi, pos4, part,
+            [&](int j) {
+                const float4 pj = pos4[j];
+                const float3 dpij = pi - xyz(pj);
+                const float ldp = len3(dpij);
+                const float wij = poly6(S, ldp);
+                const float adij = adhesionSpline(S, ldp);
+                const float mj = -pj.w;
+                const float3 a = bezier(S.adhG, aux4[j].z) * mi * mj * adij * dpij / fmaxf(kEps, ldp);
+                const float vj = mj / vel4[j].w;
+                Terms<4> t;
+                t.v[0] = a.x;
+                t.v[1] = a.y;
+                t.v[2] = a.z;
+                t.v[3] = vj * wij;
+                return t;
+            },
+            [&](const Terms<4>& t) {
+                ad += mk3(t.v[0], t.v[1], t.v[2]);
+                v_s += t.v[3];
+            });
+        if (part != 0) return;
         adh4[slot] = make_float4(ad.x, ad.y, ad.z, v_s);  // w: the average's denominator, for the adjoint
         const float3 avg = v_s != 0.f ? ad / v_s : mk3(0.f, 0.f, 0.f);
         avgadh4[slot] = make_float4(avg.x, avg.y, avg.z, 0.f);
@@ -753,14 +808,30 @@ void launchDensity(const LaunchCtx& c, const PassBuffers& b) {
                                                         b.vel4, b.aux4);
 }
 
+template <int G> void launchAvgFlowG(const LaunchCtx& c, const PassBuffers& b) {
+    kAvgFlow<G><<<grid(c, kPassAvgFlow) * G, c.block[kPassAvgFlow], 0, c.stream>>>(c.scenes, c.blockScene, b.lists,
+                                                                                  b.pos4, b.vel4, b.aux4, b.flow4);
+}
 void launchAvgFlow(const LaunchCtx& c, const PassBuffers& b) {
-    kAvgFlow<<<grid(c, kPassAvgFlow), c.block[kPassAvgFlow], 0, c.stream>>>(c.scenes, c.blockScene, b.lists, b.pos4, b.vel4, b.aux4,
-                                                        b.flow4);
+    switch (c.lanes) {
+    case 2: launchAvgFlowG<2>(c, b); break;
+    case 4: launchAvgFlowG<4>(c, b); break;
+    case 8: launchAvgFlowG<8>(c, b); break;
+    default: launchAvgFlowG<1>(c, b); break;
+    }
 }
 
+template <int G> void launchVoidageAdhesionG(const LaunchCtx& c, const PassBuffers& b) {
+    kVoidageAdhesion<G><<<grid(c, kPassVoidage) * G, c.block[kPassVoidage], 0, c.stream>>>(
+        c.scenes, c.blockScene, b.lists, b.pos4, b.vel4, b.aux4, b.adh4, b.avgadh4, b.col4, b.dp);
+}
 void launchVoidageAdhesion(const LaunchCtx& c, const PassBuffers& b) {
-    kVoidageAdhesion<<<grid(c, kPassVoidage), c.block[kPassVoidage], 0, c.stream>>>(c.scenes, c.blockScene, b.lists, b.pos4, b.vel4,
-                                                                b.aux4, b.adh4, b.avgadh4, b.col4, b.dp);
+    switch (c.lanes) {
+    case 2: launchVoidageAdhesionG<2>(c, b); break;
+    case 4: launchVoidageAdhesionG<4>(c, b); break;
+    case 8: launchVoidageAdhesionG<8>(c, b); break;
+    default: launchVoidageAdhesionG<1>(c, b); break;
+    }
 }
 
 template <int G> void launchSandMomentumG(const LaunchCtx& c, const PassBuffers& b) {

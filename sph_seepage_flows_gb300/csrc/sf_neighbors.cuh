@@ -107,6 +107,50 @@ __device__ __forceinline__ void forBoundaryNeighbors(const SceneDev& S, const Nb
     }
 }
 
+// N floats of one neighbour's terms.
+template <int N> struct Terms {
+    float v[N];
+};
+
+// The neighbours of one label, with sums that must keep the single-thread
+// order: in rounds of G list entries, lane `part` evaluates term(j) of entry
+// round * G + part, then every lane folds the round's G terms in entry order
+// (fold(t) adds t's floats to the accumulators). Every lane ends with the
+// same sums, formed with the same operations in the same order as one
+// thread walking the list, so G only changes how many threads share the
+// term evaluations. An overflowed list is walked in full by every lane.
+template <bool kSand, int G, int N, typename Term, typename Fold>
+__device__ __forceinline__ void forLabelNeighborsOrdered(const SceneDev& S, const NbrLists& L, int slot, float3 pi,
+                                                         const float4* __restrict__ pos4, int part, Term&& term,
+                                                         Fold&& fold) {
+    const unsigned c = L.cnt[slot];
+    if (G == 1 || int(c & 0xFFFFu) + int(c >> 16) > L.cap) {
+        forLabelNeighbors<kSand>(S, L, slot, pi, pos4, [&](int j) { fold(term(j)); });
+        return;
+    }
+    const int n = kSand ? int(c & 0xFFFFu) : int(c >> 16);
+    const unsigned* __restrict__ p = L.nbr + slot + (kSand ? 0 : size_t(L.cap - 1) * L.M);
+    const long long step = kSand ? L.M : -L.M;
+    const unsigned lane = threadIdx.x & 31u, base = lane & ~unsigned(G - 1);
+    const unsigned mask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << base;
+    for (int k0 = 0; k0 < n; k0 += G) {
+        Terms<N> t;
+        if (k0 + part < n) {
+            t = term(int(p[(k0 + part) * step]));
+        } else {
+#pragma unroll
+            for (int q = 0; q < N; ++q) t.v[q] = 0.f;
+        }
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            Terms<N> u;
+#pragma unroll
+            for (int q = 0; q < N; ++q) u.v[q] = __shfl_sync(mask, t.v[q], int(base) + g);
+            if (k0 + g < n) fold(u);
+        }
+    }
+}
+
 // Sum over the G lanes of a slot (G consecutive lanes of one warp, G divides
 // 32; all G lanes call it).
 template <int G> __device__ __forceinline__ float groupSum(float v) {
