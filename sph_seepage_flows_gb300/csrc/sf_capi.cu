@@ -217,6 +217,12 @@ struct sf_handle {
     AdjBuffers adj{};
     float* adjTarget = nullptr;   // 3 floats per slot, indexed by slot_off + id
     float* adjParam = nullptr;    // 3 per block of the adjoint pair kernels (lanes per slot block)
+    // captured store-mode substeps of the adjoint, per buffer set and stored
+    // substep slot, for the slab buffer they were captured with
+    std::vector<GraphCache> storeGraph[2];
+    // captured reverse substeps, per stored substep slot
+    std::vector<GraphCache> adjGraph;
+    char* storeGraphSlab = nullptr;
     float2* adjLoss = nullptr;    // 1 per slot block
     char* snap = nullptr;         // state snapshots for checkpointing
     size_t snapBytes = 0;
@@ -296,6 +302,15 @@ struct sf_handle {
             g.dt = 0.f;
             g.nodes = 0;
         }
+        for (auto& v : storeGraph) {
+            for (auto& g : v)
+                if (g.exec) cudaGraphExecDestroy(g.exec);
+            v.clear();
+        }
+        for (auto& g : adjGraph)
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+        adjGraph.clear();
+        storeGraphSlab = nullptr;
     }
     ~sf_handle() {
         for (auto& g : graph)
@@ -1427,6 +1442,85 @@ sf_status runSubstepStore(sf_handle* h, float dt, const AdjSlab& s) {
     return runStage(h, SF_STAGE_INTEGRATE, dt, 0);
 }
 
+// One store-mode substep into stored-substep slot t, replayed from a graph
+// captured per buffer set and slot on first use (and again when dt or the
+// slab buffer changes): the ~20 launches of a substep cost more than the
+// kernels themselves on small scenes.
+sf_status runSubstepStoreGraphed(sf_handle* h, float dt, int64_t t) {
+    if (h->storeGraphSlab != h->slab) {
+        h->dropGraphs();
+        h->storeGraphSlab = h->slab;
+    }
+    std::vector<GraphCache>& v = h->storeGraph[h->cur];
+    if (int64_t(v.size()) <= t) v.resize(size_t(t) + 1);
+    GraphCache& g = v[size_t(t)];
+    if (!g.exec || g.dt != dt) {
+        if (g.exec) {
+            cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+        }
+        const int curBefore = h->cur;
+        const int64_t launchesBefore = h->launches;
+        cudaGraph_t graph = nullptr;
+        sf_status st = h->cuda(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        if (st) return st;
+        st = runSubstepStore(h, dt, slabAt(h, h->slab + size_t(t) * slabStride(h)));
+        cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+        h->cur = curBefore;
+        g.nodes = int(h->launches - launchesBefore);
+        h->launches = launchesBefore;
+        if (st != SF_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return st;
+        }
+        if (h->cuda(ce, "end capture")) return SF_ERR_CUDA;
+        st = h->cuda(cudaGraphInstantiate(&g.exec, graph, 0), "graph instantiate");
+        cudaGraphDestroy(graph);
+        if (st) return st;
+        g.dt = dt;
+    }
+    if (h->cuda(cudaGraphLaunch(g.exec, h->stream), "graph launch")) return SF_ERR_CUDA;
+    h->launches += g.nodes;
+    h->cur = 1 - h->cur;
+    h->sorted = true;
+    return SF_OK;
+}
+
+// The reverse substep of stored-substep slot t, replayed from a graph
+// captured per slot (the adjoint buffers, partials and slabs are fixed).
+sf_status runAdjSubstepGraphed(sf_handle* h, float dt, int64_t t) {
+    if (h->storeGraphSlab != h->slab) {
+        h->dropGraphs();
+        h->storeGraphSlab = h->slab;
+    }
+    if (int64_t(h->adjGraph.size()) <= t) h->adjGraph.resize(size_t(t) + 1);
+    GraphCache& g = h->adjGraph[size_t(t)];
+    if (!g.exec || g.dt != dt) {
+        if (g.exec) {
+            cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+        }
+        cudaGraph_t graph = nullptr;
+        sf_status st = h->cuda(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        if (st) return st;
+        const AdjSlab sl = slabAt(h, h->slab + size_t(t) * slabStride(h));
+        g.nodes = launchAdjSubstep(h->ctx(), h->adj, slabBuffers(h, sl), sl.pid, dt, h->adjParam, h->lanes);
+        const cudaError_t le = cudaGetLastError();
+        const cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+        if (h->cuda(le, "adjoint launch") || h->cuda(ce, "end capture")) {
+            if (graph) cudaGraphDestroy(graph);
+            return SF_ERR_CUDA;
+        }
+        st = h->cuda(cudaGraphInstantiate(&g.exec, graph, 0), "graph instantiate");
+        cudaGraphDestroy(graph);
+        if (st) return st;
+        g.dt = dt;
+    }
+    if (h->cuda(cudaGraphLaunch(g.exec, h->stream), "graph launch")) return SF_ERR_CUDA;
+    h->launches += g.nodes;
+    return SF_OK;
+}
+
 sf_status growBuffer(sf_handle* h, char*& p, size_t& have, size_t need, const char* what) {
     if (have >= need) return SF_OK;
     if (p && h->cuda(cudaStreamSynchronize(h->stream), "sync before realloc")) return SF_ERR_CUDA;
@@ -1476,9 +1570,8 @@ sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t che
     const int64_t lastLen = T - (nSeg - 1) * K;
     // snapshots: segment starts [0, nSeg - 1) and the final state; slabs: one segment
     if (ensureAdjoint(h, size_t(nSeg), size_t(K))) return SF_ERR_CUDA;
-    const size_t sStride = snapStride(h), lStride = slabStride(h);
+    const size_t sStride = snapStride(h);
     auto snapAt = [&](int64_t k) { return h->snap + size_t(k) * sStride; };
-    auto slab = [&](int64_t t) { return slabAt(h, h->slab + size_t(t) * lStride); };
     char* finalSnap = snapAt(nSeg - 1);
 
     // targets into the slot_off + id layout
@@ -1511,7 +1604,7 @@ sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t che
         if ((st = sf_substeps_fixed(h, dt, K))) return st;
     }
     for (int64_t t = 0; t < lastLen; ++t)
-        if ((st = runSubstepStore(h, dt, slab(t)))) return st;
+        if ((st = runSubstepStoreGraphed(h, dt, t))) return st;
     launchAdjSeed(h->ctx(), h->pos[h->cur], h->pid[h->cur], h->adjTarget, h->adj.adjX, h->adj.adjV, h->adjLoss);
     h->launches += 1;
     if ((st = snapCopy(h, finalSnap, true))) return st;
@@ -1527,13 +1620,10 @@ sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t che
         if (seg != nSeg - 1) {
             if ((st = snapCopy(h, snapAt(seg), false))) return st;
             for (int64_t t = 0; t < len; ++t)
-                if ((st = runSubstepStore(h, dt, slab(t)))) return st;
+                if ((st = runSubstepStoreGraphed(h, dt, t))) return st;
         }
-        for (int64_t t = len - 1; t >= 0; --t) {
-            const AdjSlab sl = slab(t);
-            h->launches += launchAdjSubstep(h->ctx(), h->adj, slabBuffers(h, sl), sl.pid, dt, h->adjParam, h->lanes);
-            if (h->cuda(cudaGetLastError(), "adjoint launch")) return SF_ERR_CUDA;
-        }
+        for (int64_t t = len - 1; t >= 0; --t)
+            if ((st = runAdjSubstepGraphed(h, dt, t))) return st;
     }
     cudaEventRecord(ev[2], h->stream);
     if ((st = snapCopy(h, finalSnap, false))) return st;
