@@ -313,6 +313,217 @@ __global__ void __launch_bounds__(kSlotAlign, 6) kDensity(const SceneDev* __rest
     aux4[slot].x = pressure;
 }
 
+// The density pass with G lanes per slot (small scenes), with lists, counts,
+// density and pressure identical to kDensity's. The 32-candidate chunks of
+// the stencil walk, in stencil order, are dealt round-robin to the lanes; in
+// each round every lane tests its chunk at the same time, and the round's
+// hits are appended at the positions a single thread would have given them
+// (prefix counts over the lanes in chunk order, then the rank within the
+// chunk). Boundary candidates and the entries of the contact filter are
+// dealt one per lane and ranked by a ballot; the water density folds the
+// round's terms in list order. The rare paths (water with boundary
+// neighbours, overflowed lists) run in lane 0.
+template <int G>
+__global__ void __launch_bounds__(kSlotAlign) kDensityLanes(const SceneDev* __restrict__ scenes,
+                                                            const int* __restrict__ blockScene,
+                                                            SceneState* __restrict__ state, NbrListsW L,
+                                                            const float4* __restrict__ pos4,
+                                                            const float4* __restrict__ bpos4,
+                                                            float4* __restrict__ vel4, float4* __restrict__ aux4) {
+    SF_SLOT_PROLOGUE_G
+    if (part == 0 && slot == S.slot_off) state[sid].amax_bits = 0u;
+    const float4 pi4 = pos4[slot];
+    if (pi4.w == 0.f) return;
+    const float3 pi = xyz(pi4);
+    const int3 c = cellOf(S, pi);
+    const bool water = pi4.w > 0.f;
+    const long long M = L.M;
+    unsigned* __restrict__ nb = L.nbr + slot;
+    const unsigned lane = threadIdx.x & 31u, gbase = lane & ~unsigned(G - 1);
+    const unsigned gmask = ((1u << G) - 1u) << gbase;
+    int cS = 0, cW = 0;
+    const int z0 = max(c.z - 1, 0), z1 = min(c.z + 1, S.gz - 1) + 1;
+    unsigned myJ0 = 0u, myHit = 0u, mySand = 0u;
+    // appends the round's hits at their single-thread positions
+    auto flush = [&]() {
+        const int ns = __popc(myHit & mySand), nw = __popc(myHit & ~mySand);
+        int ps = ns, pw = nw;  // inclusive prefix over the lanes, in chunk order
+#pragma unroll
+        for (int o = 1; o < G; o <<= 1) {
+            const int ts = __shfl_up_sync(gmask, ps, o, G), tw = __shfl_up_sync(gmask, pw, o, G);
+            if (part >= o) {
+                ps += ts;
+                pw += tw;
+            }
+        }
+        ps -= ns;
+        pw -= nw;
+        for (unsigned m = myHit; m; m &= m - 1u) {
+            const int t = __ffs(m) - 1;
+            const unsigned low = myHit & ((1u << t) - 1u);
+            if (cS + cW + ps + pw + __popc(low) < L.cap) {  // the single thread's overflow test
+                if ((mySand >> t) & 1u)
+                    nb[(cS + ps + __popc(low & mySand)) * M] = myJ0 + unsigned(t);
+                else
+                    nb[(L.cap - 1 - (cW + pw + __popc(low & ~mySand))) * M] = myJ0 + unsigned(t);
+            }
+        }
+        // round totals: the last lane's inclusive prefix
+        cS += __shfl_sync(gmask, ps + ns, int(gbase) + G - 1);
+        cW += __shfl_sync(gmask, pw + nw, int(gbase) + G - 1);
+        myHit = mySand = 0u;
+    };
+    // the 9 column ranges of the stencil (particles and boundary), loaded
+    // together up front: on a small scene the walk is a latency chain
+    unsigned cb[9], ce[9], bb[9], be[9];
+#pragma unroll
+    for (int m = 0; m < 9; ++m) {
+        const int x = c.x + m / 3 - 1, y = c.y + m % 3 - 1;
+        cb[m] = ce[m] = bb[m] = be[m] = 0u;
+        if (x >= 0 && x < S.gx && y >= 0 && y < S.gy) {
+            const int base = S.cell_off + (x * S.gy + y) * S.gz;
+            cb[m] = L.cs[base + z0];
+            ce[m] = L.cs[base + z1];
+            bb[m] = L.bcs[base + z0];
+            be[m] = L.bcs[base + z1];
+        }
+    }
+    // chunk q of the stencil order: column m with pre[m] <= q < pre[m + 1]
+    int pre[10];
+    pre[0] = 0;
+#pragma unroll
+    for (int m = 0; m < 9; ++m) pre[m + 1] = pre[m] + int((ce[m] - cb[m] + 31u) / 32u);
+    const int nq = pre[9];
+    // round r: lane part tests chunk r * G + part (all lanes at once)
+#pragma unroll 1
+    for (int r0 = 0; r0 < nq; r0 += G) {
+        const int qq = r0 + part;
+        if (qq < nq) {
+            unsigned j0 = 0u, jEnd = 0u;
+#pragma unroll
+            for (int m = 0; m < 9; ++m)
+                if (qq >= pre[m] && qq < pre[m + 1]) {
+                    j0 = cb[m] + 32u * unsigned(qq - pre[m]);
+                    jEnd = ce[m];
+                }
+            const int n = int(min(32u, jEnd - j0));
+            unsigned rev = 0u, srev = 0u;
+#pragma unroll 8
+            for (int t = 0; t < n; ++t) {
+                const float4 qv = pos4[j0 + unsigned(t)];
+                rev = __funnelshift_l(__float_as_uint(reachSign(S, pi - xyz(qv))), rev, 1);
+                srev = __funnelshift_l(__float_as_uint(qv.w), srev, 1);
+            }
+            if (n > 0) {  // always, as every chunk index maps to a non-empty column
+                myJ0 = j0;
+                myHit = __brev(rev) >> (32 - n);
+                mySand = __brev(srev) >> (32 - n);
+            }
+        }
+        flush();
+    }
+    __syncwarp(gmask);  // the group's list entries are visible to every lane
+    const bool listed = cS + cW <= L.cap;
+    int bc = 0;
+    {
+        // boundary candidates dealt to the lanes one at a time, in stencil
+        // order; a ballot ranks the hits
+        unsigned* __restrict__ bnb = L.bnbr + slot;
+#pragma unroll
+        for (int m = 0; m < 9; ++m) {
+#pragma unroll 1
+            for (unsigned j0 = bb[m]; j0 < be[m]; j0 += unsigned(G)) {
+                const unsigned j = j0 + unsigned(part);
+                const bool in = j < be[m] && inReachFast(S, pi - xyz(bpos4[j]));
+                const unsigned ball = __ballot_sync(gmask, in) >> gbase;
+                if (in) {
+                    const int r = bc + __popc(ball & ((1u << part) - 1u));
+                    if (r < kMaxBNbr) bnb[r * M] = j;
+                }
+                bc += __popc(ball);
+            }
+        }
+    }
+    int cc = 0;
+    if (!water) {
+        unsigned* __restrict__ cnb = L.cnbr + slot;
+        if (listed) {
+            for (int k0 = 0; k0 < cS; k0 += G) {
+                const int k = k0 + part;
+                bool in = false;
+                unsigned j = 0u;
+                if (k < cS) {
+                    j = nb[k * M];
+                    if (j != unsigned(slot)) {
+                        const float3 dij = pi - xyz(pos4[j]);
+                        in = dot3(dij, dij) < S.dem_reach2;
+                    }
+                }
+                const unsigned ball = __ballot_sync(gmask, in) >> gbase;
+                if (in) {
+                    const int r = cc + __popc(ball & ((1u << part) - 1u));
+                    if (r < kMaxContact) cnb[r * M] = j;
+                }
+                cc += __popc(ball);
+            }
+        } else if (part == 0) {
+            for (int x = max(c.x - 1, 0); x <= min(c.x + 1, S.gx - 1); ++x)
+                for (int y = max(c.y - 1, 0); y <= min(c.y + 1, S.gy - 1); ++y) {
+                    const int base = S.cell_off + (x * S.gy + y) * S.gz;
+                    for (unsigned j = L.cs[base + z0]; j < L.cs[base + z1]; ++j) {
+                        const float4 pj = pos4[j];
+                        if (!(pj.w < 0.f) || !inReachFast(S, pi - xyz(pj)) || j == unsigned(slot)) continue;
+                        const float3 dij = pi - xyz(pj);
+                        if (dot3(dij, dij) < S.dem_reach2) {
+                            if (cc < kMaxContact) cnb[cc * M] = j;
+                            ++cc;
+                        }
+                    }
+                }
+        }
+    }
+    float density = S.rho1;
+    if (water) {
+        if (listed && bc == 0) {
+            // m_i W(0), then the water list in order, G entries per round
+            float d = pi4.w * S.W0;
+            const unsigned* __restrict__ wp = L.nbr + slot + size_t(L.cap - 1) * M;
+            for (int k0 = 0; k0 < cW; k0 += G) {
+                float t = 0.f;
+                if (k0 + part < cW) {
+                    const float4 pj = pos4[wp[-(k0 + part) * M]];
+                    t = pj.w * poly6(S, len3(pi - xyz(pj)));
+                }
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    const float u = __shfl_sync(gmask, t, int(gbase) + g);
+                    if (k0 + g < cW) d += u;
+                }
+            }
+            density = d;
+        } else if (part == 0) {
+            density = listed && bc <= kMaxBNbr ? listDensity(S, L, slot, cW, bc, pi, pi4.w, pos4, bpos4)
+                                               : exactDensity(S, L, pi, pi4.w, pos4, bpos4);
+        }
+    }
+    if (part != 0) return;
+    L.cnt[slot] = unsigned(min(cS, 0xFFFF)) | (unsigned(min(cW, 0xFFFF)) << 16);
+    L.bcnt[slot] = bc;
+    L.ccnt[slot] = cc;
+    float pressure = 0.f;
+    if (water) {
+        if (S.tait) {
+            pressure = S.stiff * (powf(density / S.rho0, 7.f) - 1.f);
+            if (pressure < 0.f) pressure *= S.neg_scale;
+        } else {
+            pressure = S.stiff * (density - S.rho0);
+            if (pressure < 0.f) pressure *= 1.f;
+        }
+    }
+    vel4[slot].w = density;
+    aux4[slot].x = pressure;
+}
+
 // ------------------------------------------------------------ avg-flow stage
 // ComputeSFAvgFlow_CUDA with ComputeSFSandVolume and ComputeSFAvgFlow
 // (cuda_sph_sf_solver_gpu.cuh:111-173, 510-572). The two sub-loops feed
@@ -803,9 +1014,21 @@ void launchBoundaryVolume(const LaunchCtx& c, int sid, int nb, float4* bpos4, co
     kBoundaryVolume<<<(nb + 255) / 256, 256, 0, c.stream>>>(c.scenes, sid, bpos4, blabel, bcs);
 }
 
+template <int G> void launchDensityLanes(const LaunchCtx& c, const PassBuffers& b) {
+    kDensityLanes<G><<<grid(c, kPassDensity) * G, c.block[kPassDensity], 0, c.stream>>>(
+        c.scenes, c.blockScene, c.state, b.listsW, b.pos4, b.bpos4, b.vel4, b.aux4);
+}
 void launchDensity(const LaunchCtx& c, const PassBuffers& b) {
-    kDensity<<<grid(c, kPassDensity), c.block[kPassDensity], 0, c.stream>>>(c.scenes, c.blockScene, c.state, b.listsW, b.pos4, b.bpos4,
-                                                        b.vel4, b.aux4);
+    switch (c.lanes) {
+    case 2: launchDensityLanes<2>(c, b); break;
+    case 4: launchDensityLanes<4>(c, b); break;
+    case 8: launchDensityLanes<8>(c, b); break;
+    default:
+        kDensity<<<grid(c, kPassDensity), c.block[kPassDensity], 0, c.stream>>>(c.scenes, c.blockScene, c.state,
+                                                                                b.listsW, b.pos4, b.bpos4, b.vel4,
+                                                                                b.aux4);
+        break;
+    }
 }
 
 template <int G> void launchAvgFlowG(const LaunchCtx& c, const PassBuffers& b) {
