@@ -600,7 +600,15 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
     SF_ALLOC(h->sc.keysAlt, sizeof(unsigned) * M);
     SF_ALLOC(h->sc.vals, sizeof(unsigned) * M);
     SF_ALLOC(h->sc.valsAlt, sizeof(unsigned) * M);
-    h->sc.tiles = sortTiles(h->totalSlots);
+    {
+        int dev = 0, sms = 0;
+        if (h->cuda(cudaGetDevice(&dev), "cudaGetDevice") ||
+            h->cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"))
+            return bail(SF_ERR_CUDA);
+        h->sc.items = sortItemsFor(h->totalSlots, sms);
+        h->lanes = lanesForSlots(h->totalSlots, sms);
+    }
+    h->sc.tiles = sortTiles(h->totalSlots, h->sc.items);
     SF_ALLOC(h->sc.hist, sizeof(unsigned) * 256 * size_t(h->sc.tiles));
     SF_ALLOC(h->sc.digitTotal, sizeof(unsigned) * 256);
     SF_ALLOC(h->cs, sizeof(unsigned) * (size_t(h->totalCells) + 1));
@@ -688,13 +696,6 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
     }
     if (h->cuda(cudaGetLastError(), "boundary volume") || h->cuda(cudaStreamSynchronize(h->stream), "create sync"))
         return bail(SF_ERR_CUDA);
-    {
-        int dev = 0, sms = 0;
-        if (h->cuda(cudaGetDevice(&dev), "cudaGetDevice") ||
-            h->cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"))
-            return bail(SF_ERR_CUDA);
-        h->lanes = lanesForSlots(h->totalSlots, sms);
-    }
     // neighbour list capacity from the initial neighbour counts
     if (probeListCapacity(h) != SF_OK) return bail(SF_ERR_CUDA);
     *out = h;

@@ -115,9 +115,15 @@ struct SortScratch {
     unsigned int* valsAlt;   // n
     unsigned int* hist;      // 256 * tiles
     unsigned int* digitTotal;  // 256
-    int tiles;
+    int tiles;               // sortTiles(n, items)
+    int items;               // keys per thread of a tile: 1, 2, 4 or 8 (0 means 8)
 };
-int sortTiles(int n);
+// Tiles of 256 threads x items keys over n keys.
+int sortTiles(int n, int items = 8);
+// Keys per thread for n keys: the largest of 8, 4, 2 that still gives every
+// SM two tiles, else 1 (small sorts are a chain of short launches; smaller
+// tiles spread them over more SMs).
+int sortItemsFor(int n, int smCount);
 // Sorts keys[0..n) (only the low `bits` bits are examined) and writes the
 // stable permutation to *permOut (new index -> old index) and the sorted keys
 // to *keysOut; both point into keys/scratch buffers. Returns kernels launched.

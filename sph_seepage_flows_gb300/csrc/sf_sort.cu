@@ -18,13 +18,19 @@
 namespace sfg {
 
 constexpr int kSortThreads = 256;
-constexpr int kSortItems = 8;
-constexpr int kTile = kSortThreads * kSortItems;
 
-int sortTiles(int n) { return (n + kTile - 1) / kTile; }
+int sortTiles(int n, int items) { return (n + kSortThreads * items - 1) / (kSortThreads * items); }
 
+int sortItemsFor(int n, int smCount) {
+    for (int items = 8; items > 1; items >>= 1)
+        if (sortTiles(n, items) >= 2 * smCount) return items;
+    return 1;
+}
+
+template <int kSortItems>
 __global__ void __launch_bounds__(kSortThreads) kHist(const unsigned int* __restrict__ keys, int n, int shift,
                                                       unsigned int* __restrict__ hist, int tiles) {
+    constexpr int kTile = kSortThreads * kSortItems;
     __shared__ unsigned int h[256];
     h[threadIdx.x] = 0;
     __syncthreads();
@@ -63,6 +69,7 @@ __global__ void __launch_bounds__(kSortThreads) kScanTiles(unsigned int* __restr
     if (threadIdx.x == 0) digitTotal[blockIdx.x] = carry;
 }
 
+template <int kSortItems>
 __global__ void __launch_bounds__(kSortThreads) kScatter(const unsigned int* __restrict__ keysIn,
                                                          const unsigned int* __restrict__ valsIn,
                                                          unsigned int* __restrict__ keysOut,
@@ -70,6 +77,7 @@ __global__ void __launch_bounds__(kSortThreads) kScatter(const unsigned int* __r
                                                          const unsigned int* __restrict__ hist, int tiles,
                                                          const unsigned int* __restrict__ digitTotal) {
     constexpr int kWarps = kSortThreads / 32;
+    constexpr int kTile = kSortThreads * kSortItems;
     __shared__ unsigned int base[256];
     __shared__ unsigned int running[256];
     __shared__ unsigned int cnt[kWarps][256];
@@ -124,9 +132,18 @@ __global__ void __launch_bounds__(kSortThreads) kScatter(const unsigned int* __r
     }
 }
 
+template <int kSortItems>
+static void launchPass(cudaStream_t s, int n, int shift, const unsigned int* kIn, const unsigned int* vIn,
+                       unsigned int* kOut, unsigned int* vOut, const SortScratch& sc) {
+    const int tiles = sc.tiles;
+    kHist<kSortItems><<<tiles, kSortThreads, 0, s>>>(kIn, n, shift, sc.hist, tiles);
+    kScanTiles<<<256, kSortThreads, 0, s>>>(sc.hist, tiles, sc.digitTotal);
+    kScatter<kSortItems><<<tiles, kSortThreads, 0, s>>>(kIn, vIn, kOut, vOut, n, shift, sc.hist, tiles,
+                                                        sc.digitTotal);
+}
+
 int radixSort(cudaStream_t s, int n, int bits, unsigned int* keys, SortScratch& sc, unsigned int** keysOut,
               unsigned int** permOut) {
-    const int tiles = sortTiles(n);
     const int passes = (bits + 7) / 8;
     unsigned int* kIn = keys;
     unsigned int* kOut = sc.keysAlt;
@@ -135,9 +152,12 @@ int radixSort(cudaStream_t s, int n, int bits, unsigned int* keys, SortScratch& 
     int launches = 0;
     for (int p = 0; p < passes; ++p) {
         const int shift = 8 * p;
-        kHist<<<tiles, kSortThreads, 0, s>>>(kIn, n, shift, sc.hist, tiles);
-        kScanTiles<<<256, kSortThreads, 0, s>>>(sc.hist, tiles, sc.digitTotal);
-        kScatter<<<tiles, kSortThreads, 0, s>>>(kIn, vIn, kOut, vOut, n, shift, sc.hist, tiles, sc.digitTotal);
+        switch (sc.items) {
+        case 1: launchPass<1>(s, n, shift, kIn, vIn, kOut, vOut, sc); break;
+        case 2: launchPass<2>(s, n, shift, kIn, vIn, kOut, vOut, sc); break;
+        case 4: launchPass<4>(s, n, shift, kIn, vIn, kOut, vOut, sc); break;
+        default: launchPass<8>(s, n, shift, kIn, vIn, kOut, vOut, sc); break;
+        }
         launches += 3;
         // next pass reads what this one wrote
         unsigned int* t = kIn;
