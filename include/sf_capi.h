@@ -257,6 +257,15 @@ sf_status sf_launch_count(const sf_handle* h, int64_t* launches);
  * value. Takes effect at the next substep (captured graphs are dropped). */
 sf_status sf_set_tuning(sf_handle* h, int32_t block_size, int32_t items_per_thread);
 
+/* Threads per particle of the neighbour passes and of the adjoint pair
+ * kernels (no reference counterpart): 1, 2, 4 or 8, or 0 for the automatic
+ * choice (doubled up to 8 while fewer than 2048 threads per SM would run,
+ * i.e. 1 for large scenes). The density, average-flow and voidage/adhesion
+ * results and the neighbour lists are the same for every value; the
+ * momentum sums are grouped differently (FP32 rounding only). Takes effect
+ * at the next substep (captured graphs are dropped). */
+sf_status sf_set_lanes(sf_handle* h, int32_t lanes);
+
 /* Autotuner (no reference counterpart). Sizes the neighbour lists for the
  * current state (list capacity = largest neighbour count + 25%, a multiple of
  * 32 in [64, 256]; sf_create does this once for the initial state) and picks

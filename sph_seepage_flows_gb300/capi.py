@@ -80,6 +80,7 @@ def load(path: str = LIB_PATH):
         "sf_synchronize": (i32, [H]),
         "sf_launch_count": (i32, [H, P(i64)]),
         "sf_set_tuning": (i32, [H, i32, i32]),
+        "sf_set_lanes": (i32, [H, i32]),
         "sf_autotune": (i32, [H, f32, P(i32), P(i32)]),
         "sf_last_error_string": (ctypes.c_char_p, [H]),
         "sf_adjoint_run": (i32, [H, f32, i64, i64, P(f32), P(f32), P(f32), P(f32), P(f32), P(f32)]),
@@ -250,6 +251,10 @@ class Simulation:
 
     def set_tuning(self, block_size: int, items_per_thread: int = 0):
         self._check(self.lib.sf_set_tuning(self.h, int(block_size), int(items_per_thread)))
+
+    def set_lanes(self, lanes: int):
+        """sf_set_lanes: threads per particle of the neighbour passes (0 = automatic)."""
+        self._check(self.lib.sf_set_lanes(self.h, int(lanes)))
 
     def autotune(self, dt: float) -> dict:
         """sf_autotune: list capacity and per-pass block sizes for the current state."""

@@ -240,6 +240,7 @@ struct sf_handle {
         return SF_ERR_CUDA;
     }
     int adjBlocks() const { return slotBlocks * lanes; }
+    static constexpr int kMaxLanes = 8;
     LaunchCtx ctx() const {
         LaunchCtx c;
         c.stream = stream;
@@ -1257,6 +1258,22 @@ sf_status sf_set_tuning(sf_handle* h, int32_t block_size, int32_t items_per_thre
     return SF_OK;
 }
 
+sf_status sf_set_lanes(sf_handle* h, int32_t lanes) {
+    if (!h) return SF_ERR_INVALID;
+    if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8)
+        return h->fail(SF_ERR_INVALID, "lanes must be 0 (automatic), 1, 2, 4 or 8");
+    if (lanes == 0) {
+        int dev = 0, sms = 0;
+        if (h->cuda(cudaGetDevice(&dev), "cudaGetDevice") ||
+            h->cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count"))
+            return SF_ERR_CUDA;
+        lanes = lanesForSlots(h->totalSlots, sms);
+    }
+    h->lanes = lanes;
+    h->dropGraphs();
+    return SF_OK;
+}
+
 sf_status sf_autotune(sf_handle* h, float dt, int32_t* block_sizes_out, int32_t* list_capacity_out) {
     if (!h) return SF_ERR_INVALID;
     if (!(dt > 0.f) || !std::isfinite(dt)) return h->fail(SF_ERR_INVALID, "dt must be finite and > 0");
@@ -1542,7 +1559,8 @@ sf_status ensureAdjoint(sf_handle* h, size_t snapshots, size_t slabs) {
                 return SF_ERR_CUDA;
         }
         if (h->cuda(cudaMalloc(reinterpret_cast<void**>(&h->adjTarget), sizeof(float) * 3 * M), "cudaMalloc target") ||
-            h->cuda(cudaMalloc(reinterpret_cast<void**>(&h->adjParam), sizeof(float) * 3 * size_t(h->adjBlocks())),
+            h->cuda(cudaMalloc(reinterpret_cast<void**>(&h->adjParam),
+                               sizeof(float) * 3 * size_t(h->slotBlocks) * sf_handle::kMaxLanes),
                     "cudaMalloc param partials") ||
             h->cuda(cudaMalloc(reinterpret_cast<void**>(&h->adjLoss), sizeof(float2) * size_t(h->slotBlocks)),
                     "cudaMalloc loss partials") ||

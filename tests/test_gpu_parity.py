@@ -100,13 +100,17 @@ def dense_cluster_scene():
     return sc
 
 
+@pytest.mark.parametrize("lanes", [0, 1])
 @pytest.mark.parametrize("which", ["tiny", "dense"])
-def test_stages_bit_exact_against_fp32_oracle(cuda_lib, oracle_mod, which):
+def test_stages_bit_exact_against_fp32_oracle(cuda_lib, oracle_mod, which, lanes):
     """Each stage on identical inputs: the GPU output equals the FP32 oracle's
     bit-for-bit for every field free of powf and of reordered sums, within TOL
-    otherwise. "dense" exercises the neighbour-list overflow fallback."""
+    otherwise. "dense" exercises the neighbour-list overflow fallback. lanes 0
+    is the automatic choice for these small scenes (8 threads per particle);
+    lanes 1 is the one-thread-per-particle path that large scenes take."""
     sc = scenes.tiny(seed=11) if which == "tiny" else dense_cluster_scene()
     sim = gpu_sim(sc)
+    sim.set_lanes(lanes)
     o32 = oracle_mod.Oracle(sc, 32)
     outputs = {
         "sort": ["id", "label", "pos", "vel", "col", "mass", "radius", "cda0asat", "amcamcp", "max_saturation"],

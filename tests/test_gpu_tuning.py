@@ -1,7 +1,9 @@
 """Launch tuning (sf_set_tuning, sf_autotune) changes speed, never results:
 every pass computes each slot's outputs independently of the block shape,
 so substeps run with any block size are bit-identical. The list capacity
-probe sizes the neighbour lists so dense scenes do not overflow them."""
+probe sizes the neighbour lists so dense scenes do not overflow them. The
+lane count (sf_set_lanes: threads per particle) leaves the lists and every
+field up to the momentum passes bit-identical; the momentum sums regroup."""
 
 import numpy as np
 import pytest
@@ -60,3 +62,66 @@ def test_set_tuning_rejects_bad_sizes(cuda_lib):
             sim.set_tuning(bad)
     with pytest.raises(SfError):
         sim.set_tuning(64, 2)
+
+
+@pytest.mark.parametrize("name", ["tiny", "plain_small"])
+def test_lanes_track_one_lane(cuda_lib, name):
+    from sph_seepage_flows_gb300.capi import Simulation
+    sc = getattr(scenes, name)()
+    dt = reference_dt(sc.params, sc.bparams, sc.sparams)[1]
+    exact = ["density", "pressure", "voidage", "saturation", "avg_flow", "adhesion", "avg_adhesion", "col",
+             "max_saturation", "neighbors", "id"]
+
+    def run(lanes):
+        sim = Simulation(sc)
+        sim.set_lanes(lanes)
+        sim.substeps_fixed(dt, 3)  # three full substeps (the momentum passes regroup FP32 sums)
+        for st in ("sort", "density", "avgflow", "voidage_adhesion"):
+            sim.stage(st, dt)
+        out = {f: sim.field(f) for f in exact}
+        out["cells"] = sim.cell_table(0)
+        sim.stage("sand_momentum", dt)
+        sim.stage("water_momentum", dt)
+        out["acc"] = sim.field("acc")
+        out["pos"] = sim.field("pos")
+        sim.close()
+        return out
+
+    ref = run(1)
+    for lanes in (2, 4, 8, 0):
+        out = run(lanes)
+        # the states after three substeps differ by momentum rounding only
+        # (bit-exactness on identical inputs: the next test)
+        assert np.abs(out["pos"] - ref["pos"]).max() < 1e-5, lanes
+        scale = np.abs(ref["acc"]).max()
+        assert np.abs(out["acc"] - ref["acc"]).max() <= 1e-4 * scale, lanes
+
+
+def test_lanes_exact_on_identical_inputs(cuda_lib):
+    """From one state, the passes up to voidage/adhesion give the same bits for
+    every lane count."""
+    from sph_seepage_flows_gb300.capi import Simulation
+    sc = scenes.plain_small()
+    dt = reference_dt(sc.params, sc.bparams, sc.sparams)[1]
+    fields = ["density", "pressure", "voidage", "saturation", "avg_flow", "adhesion", "avg_adhesion", "col",
+              "max_saturation", "neighbors"]
+    outs = {}
+    for lanes in (1, 2, 4, 8):
+        sim = Simulation(sc)
+        sim.set_lanes(lanes)
+        for st in ("sort", "density", "avgflow", "voidage_adhesion"):
+            sim.stage(st, dt)
+        outs[lanes] = {f: sim.field(f) for f in fields}
+        outs[lanes]["cells"] = sim.cell_table(0)
+        sim.close()
+    for lanes in (2, 4, 8):
+        for f in outs[1]:
+            assert np.array_equal(outs[lanes][f], outs[1][f]), (lanes, f)
+
+
+def test_set_lanes_rejects_bad_counts(cuda_lib):
+    from sph_seepage_flows_gb300.capi import SfError, Simulation
+    sim = Simulation(scenes.tiny())
+    for bad in (3, 16, -1):
+        with pytest.raises(SfError):
+            sim.set_lanes(bad)
