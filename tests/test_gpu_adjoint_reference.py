@@ -40,20 +40,25 @@ def make(case):
 
 @pytest.fixture(scope="module")
 def runs(cuda_lib):
+    """Gradients with the automatic lane count (8 threads per particle on these
+    small scenes) and with one (the path of large scenes)."""
     from sph_seepage_flows_gb300.capi import Simulation
     out = {}
     for case in CASES:
-        sc, n_sub = make(case)
-        sim = Simulation(sc)
-        out[case] = (sc, n_sub, sim.adjoint(DT, n_sub, probe_target(sc)))
-        sim.close()
+        for lanes in (0, 1):
+            sc, n_sub = make(case)
+            sim = Simulation(sc)
+            sim.set_lanes(lanes)
+            out[case, lanes] = (sc, n_sub, sim.adjoint(DT, n_sub, probe_target(sc)))
+            sim.close()
     return out
 
 
+@pytest.mark.parametrize("lanes", [0, 1])
 @pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]}-{c[1]}-{c[2]}")
 @pytest.mark.parametrize("which", ["pos", "vel"] + list(PARAMS))
-def test_adjoint_against_forward_mode(runs, oracle_mod, case, which):
-    sc, n_sub, res = runs[case]
+def test_adjoint_against_forward_mode(runs, oracle_mod, case, which, lanes):
+    sc, n_sub, res = runs[case, lanes]
     target = probe_target(sc)
     if which in ("pos", "vel"):
         u = probe_direction(sc, case[1])
