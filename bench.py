@@ -127,6 +127,8 @@ def make_scene(name: str):
         return scenes.plain_small()
     if name == "tiny":
         return scenes.tiny()
+    if name == "column":  # the 20k sand column of the adjoint workload
+        return scenes.adjoint_column()
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -240,9 +242,10 @@ def adjoint_comparison(stream, n_substeps=200, checkpoint_every=20):
 
 def adjoint_workload(args):
     """--adjoint-substeps K: the gradient run on the bench workload alone (K
-    substeps, every substep stored), forward and reverse device time per
-    substep against the graph-replayed forward; used for the ncu launch list
-    of the adjoint kernels."""
+    substeps, every substep stored unless --checkpoint-every is smaller),
+    forward and reverse device time per substep against the graph-replayed
+    forward; used for the ncu launch lists of the adjoint kernels (the second
+    gradient run is bracketed by the NVTX range "timed")."""
     import torch
 
     from sph_seepage_flows_gb300 import capi
@@ -252,9 +255,10 @@ def adjoint_workload(args):
     sim = capi.Simulation(sc)
     sim.autotune(dt)
     target = sc.pos.astype(np.float32) + np.float32(1e-3)
-    sim.adjoint(dt, k, target, want_state_grads=False)  # allocates the stored substeps
+    ck = args.checkpoint_every if args.checkpoint_every > 0 else k
+    sim.adjoint(dt, k, target, checkpoint_every=ck, want_state_grads=False)  # allocates and captures
     torch.cuda.nvtx.range_push("timed")
-    r = sim.adjoint(dt, k, target, want_state_grads=False)
+    r = sim.adjoint(dt, k, target, checkpoint_every=ck, want_state_grads=False)
     torch.cuda.nvtx.range_pop()
     stream = torch.cuda.Stream()
     fwd = capi.Simulation(sc, stream=stream.cuda_stream)
@@ -266,7 +270,7 @@ def adjoint_workload(args):
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
-    print(json.dumps({"adjoint_workload": args.workload, "particles": sc.n, "substeps": k,
+    print(json.dumps({"adjoint_workload": args.workload, "particles": sc.n, "substeps": k, "checkpoint_every": ck,
                       "forward_ms_per_substep": ms / k, "store_forward_ms_per_substep": r["ms_forward"] / k,
                       "reverse_ms_per_substep": r["ms_reverse"] / k,
                       "gradient_run_vs_forward": (r["ms_forward"] + r["ms_reverse"]) / ms}), flush=True)
@@ -436,7 +440,8 @@ def run_ours(args, rank, world):
         "data": "synthetic (seeded lattice scene)",
         "config": {"workload": args.workload, "particles": n, "sand": sc.n_sand, "water": sc.n_water,
                    "boundary": sc.nb, "grid": list(sc.bparams.grid_size), "dt": dt,
-                   "l2": "working set ~250 B/particle > L2 (no flush needed)" if n >= 600_000 else "flushed",
+                   "l2": ("working set ~250 B/particle > L2 (no flush needed)" if n >= 600_000 else
+                          "working set < L2, not flushed (a profiling workload, not the benchmark)"),
                    "parallelism": f"replicas x{world}", "tuning": tuning},
         "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
@@ -474,6 +479,8 @@ def main():
     ap.add_argument("--no-calibration", action="store_true")
     ap.add_argument("--adjoint-substeps", type=int, default=0,
                     help="only time the gradient run of the workload over this many substeps")
+    ap.add_argument("--checkpoint-every", type=int, default=0,
+                    help="checkpoint interval of --adjoint-substeps (default: every substep stored)")
     args = ap.parse_args()
     if args.adjoint_substeps > 0:
         adjoint_workload(args)
