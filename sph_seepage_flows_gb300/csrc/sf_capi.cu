@@ -893,7 +893,8 @@ __global__ void kGetField(int field, int n, int slotOff, int cellOff, int order,
 
 __global__ void kSetField(int field, int n, int slotOff, int order, float4* pos, float4* vel, float4* col,
                           float4* mat, float2* amc, const int* __restrict__ pid, float4* aux, float4* flow,
-                          float4* adh, float4* avgadh, float4* drag, float4* acc, const void* in) {
+                          float4* adh, float4* avgadh, float4* drag, float4* acc, const void* in,
+                          const SceneDev* __restrict__ scene) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int s = slotOff + i;
@@ -922,7 +923,10 @@ __global__ void kSetField(int field, int n, int slotOff, int order, float4* pos,
     case SF_FIELD_DENSITY: vel[s].w = f[o]; break;
     case SF_FIELD_PRESSURE: aux[s].x = f[o]; break;
     case SF_FIELD_VOIDAGE: aux[s].w = f[o]; aux[s].y = f[o]; break;
-    case SF_FIELD_SATURATION: aux[s].z = f[o]; break;
+    case SF_FIELD_SATURATION:  // and the adhesion factor the average-flow pass derives from it
+        aux[s].z = f[o];
+        if (pos[s].w < 0.f) flow[s].w = bezier(scene->adhG, f[o]);
+        break;
     case SF_FIELD_MAX_SATURATION: col[s].w = f[o]; break;
     case SF_FIELD_AVG_FLOW: set3(flow); break;
     case SF_FIELD_AVG_DRAG: set3(drag); break;
@@ -1131,7 +1135,7 @@ sf_status sf_set_field(sf_handle* h, int32_t scene, int32_t field, int32_t order
         kSetField<<<int((n + 255) / 256), 256, 0, h->stream>>>(field, int(n), S.slot_off, order, h->pos[c],
                                                                h->vel[c], h->col[c], h->mat[c], h->amc[c], h->pid[c],
                                                                h->aux, h->flow, h->adh, h->avgadh, h->drag, h->acc,
-                                                               from);
+                                                               from, h->dScenes + scene);
     if (h->cuda(cudaGetLastError(), "set_field launch")) return SF_ERR_CUDA;
     if (!src_on_device) return h->cuda(cudaStreamSynchronize(h->stream), "set_field sync");
     return SF_OK;

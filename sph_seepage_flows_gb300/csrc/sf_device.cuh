@@ -13,7 +13,7 @@
 //       pos4  = (x, y, z, w)  w = +mass (water), -mass (sand), 0 (parking)
 //       vel4  = (vx, vy, vz, density)
 //       aux4  = (pressure, fluid voidage, saturation, voidage)
-//       flow4 = (average flow velocity, 0)
+//       flow4 = (average flow velocity, sand: adhesion Bezier factor of its saturation)
 //       adh4  = (adhesion force, 0)      avgadh4 = (average adhesion force, 0)
 //       drag4 = (average drag force, 0)  acc4    = (acceleration, 0)
 //       col4  = (colour, max saturation) mat4    = (cd, a0, asat, radius)

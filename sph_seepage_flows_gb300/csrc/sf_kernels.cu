@@ -603,7 +603,9 @@ __global__ void __launch_bounds__(kSlotAlign) kAvgFlow(const SceneDev* __restric
         avg = avg_s / v_s;
     else
         avg = mk3(0.f, 0.f, 0.f);
-    flow4[slot] = make_float4(avg.x, avg.y, avg.z, 0.f);
+    // w: the adhesion Bezier factor of a sand particle's saturation, which
+    // every water neighbour's adhesion term uses (computed once here)
+    flow4[slot] = make_float4(avg.x, avg.y, avg.z, sandI ? bezier(S.adhG, v_s) : 0.f);
     float4 a = aux4[slot];
     a.y = 1.f - sand_volume;
     a.z = v_s;
@@ -621,7 +623,8 @@ template <int G>
 __global__ void __launch_bounds__(kSlotAlign) kVoidageAdhesion(
     const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene, NbrLists L,
     const float4* __restrict__ pos4, const float4* __restrict__ vel4, float4* __restrict__ aux4,
-    float4* __restrict__ adh4, float4* __restrict__ avgadh4, float4* __restrict__ col4, float2* __restrict__ dp) {
+    const float4* __restrict__ flow4, float4* __restrict__ adh4, float4* __restrict__ avgadh4,
+    float4* __restrict__ col4, float2* __restrict__ dp) {
     SF_SLOT_PROLOGUE_G
     const float4 pi4 = pos4[slot];
     if (pi4.w == 0.f) return;
@@ -672,7 +675,7 @@ __global__ void __launch_bounds__(kSlotAlign) kVoidageAdhesion(
                 const float wij = poly6(S, ldp);
                 const float adij = adhesionSpline(S, ldp);
                 const float mj = -pj.w;
-                const float3 a = bezier(S.adhG, aux4[j].z) * mi * mj * adij * dpij / fmaxf(kEps, ldp);
+                const float3 a = flow4[j].w * mi * mj * adij * dpij / fmaxf(kEps, ldp);  // w: bezier(adhG, sat_j)
                 const float vj = mj / vel4[j].w;
                 Terms<4> t;
                 t.v[0] = a.x;
@@ -1046,7 +1049,7 @@ void launchAvgFlow(const LaunchCtx& c, const PassBuffers& b) {
 
 template <int G> void launchVoidageAdhesionG(const LaunchCtx& c, const PassBuffers& b) {
     kVoidageAdhesion<G><<<grid(c, kPassVoidage) * G, c.block[kPassVoidage], 0, c.stream>>>(
-        c.scenes, c.blockScene, b.lists, b.pos4, b.vel4, b.aux4, b.adh4, b.avgadh4, b.col4, b.dp);
+        c.scenes, c.blockScene, b.lists, b.pos4, b.vel4, b.aux4, b.flow4, b.adh4, b.avgadh4, b.col4, b.dp);
 }
 void launchVoidageAdhesion(const LaunchCtx& c, const PassBuffers& b) {
     switch (c.lanes) {
