@@ -610,7 +610,8 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
         h->lanes = lanesForSlots(h->totalSlots, sms);
     }
     h->sc.tiles = sortTiles(h->totalSlots, h->sc.items);
-    SF_ALLOC(h->sc.hist, sizeof(unsigned) * 256 * size_t(h->sc.tiles));
+    // room for the smallest tiles, so that the tuner can change the tile size
+    SF_ALLOC(h->sc.hist, sizeof(unsigned) * 256 * size_t(sortTiles(h->totalSlots, 1)));
     SF_ALLOC(h->sc.digitTotal, sizeof(unsigned) * 256);
     SF_ALLOC(h->cs, sizeof(unsigned) * (size_t(h->totalCells) + 1));
     SF_ALLOC(h->bcs, sizeof(unsigned) * (size_t(h->totalCells) + 1));
@@ -1289,37 +1290,76 @@ sf_status sf_autotune(sf_handle* h, float dt, int32_t* block_sizes_out, int32_t*
         devFree(h->slab);
         h->slabBytes = 0;
     }
-    // every pass recomputes its outputs from inputs it does not write, so
-    // repeating it on the current state is harmless; the integrator is not
-    // repeated (it advances the state) and keeps its block size
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (h->cuda(cudaEventCreate(&e0), "event") || h->cuda(cudaEventCreate(&e1), "event")) return SF_ERR_CUDA;
+    // device time of five launches of fn (after one untimed)
+    auto timed = [&](auto&& fn, float& ms) -> sf_status {
+        sf_status r = fn();
+        if (r) return r;
+        cudaEventRecord(e0, h->stream);
+        for (int k = 0; k < 5 && r == SF_OK; ++k) r = fn();
+        cudaEventRecord(e1, h->stream);
+        if (r) return r;
+        if (h->cuda(cudaEventSynchronize(e1), "tune sync") || h->cuda(cudaEventElapsedTime(&ms, e0, e1), "tune time"))
+            return SF_ERR_CUDA;
+        return SF_OK;
+    };
+    // sort tile size: sorting the sorted state again is the identity
+    {
+        float best = 0.f;
+        int bestItems = h->sc.items;
+        for (int items : {8, 4, 2, 1}) {
+            h->sc.items = items;
+            h->sc.tiles = sortTiles(h->totalSlots, items);
+            float ms = 0.f;
+            if ((st = timed([&] { return runSort(h); }, ms))) break;
+            if (best == 0.f || ms < best) {
+                best = ms;
+                bestItems = items;
+            }
+        }
+        h->sc.items = bestItems;
+        h->sc.tiles = sortTiles(h->totalSlots, bestItems);
+    }
+    // lanes per particle and the block size of every neighbour pass: every
+    // pass recomputes its outputs from inputs it does not write, so repeating
+    // it on the current state is harmless; the integrator is not repeated (it
+    // advances the state) and keeps its block size
     const int candidates[3] = {64, 128, 256};
     const int stages[kTunedPasses - 1] = {SF_STAGE_DENSITY, SF_STAGE_AVGFLOW, SF_STAGE_VOIDAGE_ADHESION,
                                           SF_STAGE_SAND_MOMENTUM, SF_STAGE_WATER_MOMENTUM};
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    if (h->cuda(cudaEventCreate(&e0), "event") || h->cuda(cudaEventCreate(&e1), "event")) return SF_ERR_CUDA;
     for (int s = SF_STAGE_DENSITY; s <= SF_STAGE_WATER_MOMENTUM && st == SF_OK; ++s) st = runStage(h, s, dt, 0);
-    for (int p = 0; p < kTunedPasses - 1 && st == SF_OK; ++p) {
-        float best = 0.f;
-        int bestBs = h->block[p];
-        for (int bs : candidates) {
-            h->block[p] = bs;
-            if ((st = runStage(h, stages[p], dt, 0))) break;
-            cudaEventRecord(e0, h->stream);
-            for (int r = 0; r < 5 && st == SF_OK; ++r) st = runStage(h, stages[p], dt, 0);
-            cudaEventRecord(e1, h->stream);
-            float ms = 0.f;
-            if (st || h->cuda(cudaEventSynchronize(e1), "tune sync") ||
-                h->cuda(cudaEventElapsedTime(&ms, e0, e1), "tune time")) {
-                st = st ? st : SF_ERR_CUDA;
-                break;
+    float bestTotal = 0.f;
+    int bestLanes = h->lanes, bestBlock[kTunedPasses - 1];
+    for (int p = 0; p < kTunedPasses - 1; ++p) bestBlock[p] = h->block[p];
+    for (int lanes : {1, 2, 4, 8}) {
+        if (st) break;
+        h->lanes = lanes;
+        float total = 0.f;
+        int block[kTunedPasses - 1];
+        for (int p = 0; p < kTunedPasses - 1 && st == SF_OK; ++p) {
+            float best = 0.f;
+            block[p] = h->block[p];
+            for (int bs : candidates) {
+                h->block[p] = bs;
+                float ms = 0.f;
+                if ((st = timed([&] { return runStage(h, stages[p], dt, 0); }, ms))) break;
+                if (best == 0.f || ms < best) {
+                    best = ms;
+                    block[p] = bs;
+                }
             }
-            if (best == 0.f || ms < best) {
-                best = ms;
-                bestBs = bs;
-            }
+            h->block[p] = block[p];
+            total += best;
         }
-        h->block[p] = bestBs;
+        if (st == SF_OK && (bestTotal == 0.f || total < bestTotal)) {
+            bestTotal = total;
+            bestLanes = lanes;
+            for (int p = 0; p < kTunedPasses - 1; ++p) bestBlock[p] = block[p];
+        }
     }
+    h->lanes = bestLanes;
+    for (int p = 0; p < kTunedPasses - 1; ++p) h->block[p] = bestBlock[p];
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (st) return st;
@@ -1327,6 +1367,15 @@ sf_status sf_autotune(sf_handle* h, float dt, int32_t* block_sizes_out, int32_t*
     if (block_sizes_out)
         for (int k = 0; k < kTunedPasses; ++k) block_sizes_out[k] = h->block[k];
     if (list_capacity_out) *list_capacity_out = h->nbrCap;
+    return SF_OK;
+}
+
+sf_status sf_get_tuning(const sf_handle* h, int32_t* block_sizes_out, int32_t* lanes_out, int32_t* sort_items_out) {
+    if (!h) return SF_ERR_INVALID;
+    if (block_sizes_out)
+        for (int k = 0; k < kTunedPasses; ++k) block_sizes_out[k] = h->block[k];
+    if (lanes_out) *lanes_out = h->lanes;
+    if (sort_items_out) *sort_items_out = h->sc.items ? h->sc.items : 8;
     return SF_OK;
 }
 
