@@ -921,7 +921,10 @@ __global__ void kSetField(int field, int n, int slotOff, int order, float4* pos,
     }
     case SF_FIELD_RADIUS: mat[s].w = f[o]; break;
     case SF_FIELD_MASS: pos[s].w = pos[s].w < 0.f ? -f[o] : f[o]; break;
-    case SF_FIELD_DENSITY: vel[s].w = f[o]; break;
+    case SF_FIELD_DENSITY:  // sand: also the copy the water momentum pass gathers with the drag
+        vel[s].w = f[o];
+        if (pos[s].w < 0.f) drag[s].w = f[o];
+        break;
     case SF_FIELD_PRESSURE: aux[s].x = f[o]; break;
     case SF_FIELD_VOIDAGE: aux[s].w = f[o]; aux[s].y = f[o]; break;
     case SF_FIELD_SATURATION:  // and the adhesion factor the average-flow pass derives from it

@@ -15,7 +15,7 @@
 //       aux4  = (pressure, fluid voidage, saturation, voidage)
 //       flow4 = (average flow velocity, sand: adhesion Bezier factor of its saturation)
 //       adh4  = (adhesion force, 0)      avgadh4 = (average adhesion force, 0)
-//       drag4 = (average drag force, 0)  acc4    = (acceleration, 0)
+//       drag4 = (average drag force, sand: density)  acc4 = (acceleration, 0)
 //       col4  = (colour, max saturation) mat4    = (cd, a0, asat, radius)
 //       amc2  = (amc, amcp)              pid     = creation index
 //   * boundary particles: bpos4 = (x, y, z, v) with v = +volume (label 0) or

@@ -791,7 +791,8 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kSandMomentum(
             df = S.grav_abs * S.rho0 * powf(eps_i, 2.f) / dragCoeff * (xyz(flow4[slot]) - vi) * mi / di;
     }
     const float3 avgDrag = v_w != 0.f ? df / v_w : mk3(0.f, 0.f, 0.f);
-    drag4[slot] = make_float4(avgDrag.x, avgDrag.y, avgDrag.z, 0.f);
+    // w: the density, which the water momentum pass gathers with the drag
+    drag4[slot] = make_float4(avgDrag.x, avgDrag.y, avgDrag.z, di);
     reinterpret_cast<float*>(dp + slot)[1] = v_w;  // the average's denominator, for the adjoint
     const float3 g = mk3(0.f, 0.f, 0.f) + mk3(S.gvx, S.gvy, S.gvz);
     const float3 a = g + 2.f * (f + df) / mi;
@@ -841,11 +842,12 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kWaterMomentum(
         forSandNeighbors<G>(S, L, slot, pi, pos4, [&](int j) {
             const float4 pj = pos4[j];
             const float3 dij = pi - xyz(pj);
-            const float dj = vel4[j].w;
+            const float4 dragj = drag4[j];  // (average drag, density)
+            const float dj = dragj.w;
             const float wij = poly6(S, len3(dij));
             const float3 nab = spikyGrad(S, dij);
             const float3 buoy = pj.w * pri / fmaxf(kEps, di * dj) * nab;  // -m_j with m_j = -w
-            const float3 drag = -wij / di * xyz(drag4[j]);
+            const float3 drag = -wij / di * xyz(dragj);
             a += buoy + drag;
         }, part);
         const float bp = pri / fmaxf(kEps, S.rho0 * S.rho0);
