@@ -750,7 +750,7 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kSandMomentum(
             if (dot3(dij, dij) < S.dem_reach2) contact(j);
         }, part);
     }
-    forWaterNeighbors<G>(S, L, slot, pi, pos4, [&](int j) {
+    forWaterNeighbors<G, true>(S, L, slot, pi, pos4, [&](int j) {
         const float4 pj = pos4[j];
         const float3 dij = pi - xyz(pj);
         const float4 aj = aux4[j];
@@ -824,7 +824,7 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kWaterMomentum(
         const float pri = aux4[slot].x;
         const float pterm_i = dpi.y;
         float3 a = mk3(0.f, 0.f, 0.f);
-        forWaterNeighbors<G>(S, L, slot, pi, pos4, [&](int j) {
+        forWaterNeighbors<G, true>(S, L, slot, pi, pos4, [&](int j) {
             if (j == slot) return;
             const float4 pj = pos4[j];
             const float3 dij = pi - xyz(pj);
@@ -839,7 +839,7 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kWaterMomentum(
                 a += -pj.w * pij * nab;
             }
         }, part);
-        forSandNeighbors<G>(S, L, slot, pi, pos4, [&](int j) {
+        forSandNeighbors<G, true>(S, L, slot, pi, pos4, [&](int j) {
             const float4 pj = pos4[j];
             const float3 dij = pi - xyz(pj);
             const float4 dragj = drag4[j];  // (average drag, density)

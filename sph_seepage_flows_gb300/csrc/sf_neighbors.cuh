@@ -32,11 +32,18 @@ __device__ __forceinline__ void forEachCell(const SceneDev& S, int3 c, F&& f) {
 
 __device__ __forceinline__ bool inReach(const SceneDev& S, float3 d) { return dot3(d, d) < S.reach2; }
 
+// A list entry; kLast marks the substep's last pass over this list, whose
+// entry loads are evict-first so that they do not push the gathered
+// per-particle arrays out of L2.
+template <bool kLast> __device__ __forceinline__ unsigned listEntry(const unsigned* __restrict__ p) {
+    return kLast ? __ldcs(p) : *p;
+}
+
 // Neighbours of one label within reach of slot, in stencil order: the sand
 // part (kSand) or the water part of the list, or the stencil when the list
 // overflowed. With G lanes per slot, lane `part` gets every G-th of them
 // starting at the part-th (G = 1: all, in order).
-template <bool kSand, int G = 1, typename F>
+template <bool kSand, int G = 1, bool kLast = false, typename F>
 __device__ __forceinline__ void forLabelNeighbors(const SceneDev& S, const NbrLists& L, int slot, float3 pi,
                                                   const float4* __restrict__ pos4, F&& f, int part = 0) {
     const unsigned c = L.cnt[slot];
@@ -48,14 +55,15 @@ __device__ __forceinline__ void forLabelNeighbors(const SceneDev& S, const NbrLi
         // consecutive entries overlap
         int k = part;
         for (; k + 3 * G < n; k += 4 * G) {
-            const int j0 = int(p[k * step]), j1 = int(p[(k + G) * step]);
-            const int j2 = int(p[(k + 2 * G) * step]), j3 = int(p[(k + 3 * G) * step]);
+            const int j0 = int(listEntry<kLast>(p + k * step)), j1 = int(listEntry<kLast>(p + (k + G) * step));
+            const int j2 = int(listEntry<kLast>(p + (k + 2 * G) * step));
+            const int j3 = int(listEntry<kLast>(p + (k + 3 * G) * step));
             f(j0);
             f(j1);
             f(j2);
             f(j3);
         }
-        for (; k < n; k += G) f(int(p[k * step]));
+        for (; k < n; k += G) f(int(listEntry<kLast>(p + k * step)));
     } else {
         // stencil walk in the same order: 9 (dx, dy) columns, 3 contiguous z-cells each
         const int3 c = cellOf(S, pi);
@@ -72,15 +80,15 @@ __device__ __forceinline__ void forLabelNeighbors(const SceneDev& S, const NbrLi
             }
     }
 }
-template <int G = 1, typename F>
+template <int G = 1, bool kLast = false, typename F>
 __device__ __forceinline__ void forSandNeighbors(const SceneDev& S, const NbrLists& L, int slot, float3 pi,
                                                  const float4* __restrict__ pos4, F&& f, int part = 0) {
-    forLabelNeighbors<true, G>(S, L, slot, pi, pos4, f, part);
+    forLabelNeighbors<true, G, kLast>(S, L, slot, pi, pos4, f, part);
 }
-template <int G = 1, typename F>
+template <int G = 1, bool kLast = false, typename F>
 __device__ __forceinline__ void forWaterNeighbors(const SceneDev& S, const NbrLists& L, int slot, float3 pi,
                                                   const float4* __restrict__ pos4, F&& f, int part = 0) {
-    forLabelNeighbors<false, G>(S, L, slot, pi, pos4, f, part);
+    forLabelNeighbors<false, G, kLast>(S, L, slot, pi, pos4, f, part);
 }
 
 // Boundary particles within reach of slot, in stencil order (lane-strided
