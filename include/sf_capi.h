@@ -270,7 +270,8 @@ sf_status sf_set_lanes(sf_handle* h, int32_t lanes);
  * current state (list capacity = largest neighbour count + 25%, a multiple of
  * 32 in [64, 256]; sf_create does this once for the initial state), then
  * times on the current state, with CUDA events: the radix sort with 8, 4, 2
- * and 1 keys per thread (tile size), and, for 1, 2, 4 and 8 threads per
+ * and 1 keys per thread (tile size) and with 8-bit or wider digits, and, for
+ * 1, 2, 4 and 8 threads per
  * particle, each neighbour pass with 64, 128 and 256 threads per block
  * (density, average flow, voidage/adhesion, sand momentum, water momentum;
  * the integrator keeps its size); it keeps the fastest sort tiles and the
@@ -281,9 +282,11 @@ sf_status sf_set_lanes(sf_handle* h, int32_t lanes);
 sf_status sf_autotune(sf_handle* h, float dt, int32_t* block_sizes_out, int32_t* list_capacity_out);
 
 /* The current launch configuration (no reference counterpart): block sizes
- * (6 entries, as sf_autotune), threads per particle of the neighbour passes
- * and keys per thread of the radix sort tiles. Any pointer may be NULL. */
-sf_status sf_get_tuning(const sf_handle* h, int32_t* block_sizes_out, int32_t* lanes_out, int32_t* sort_items_out);
+ * (6 entries, as sf_autotune), threads per particle of the neighbour passes,
+ * keys per thread of the radix sort tiles and bits per radix digit (8, or
+ * 9-11 where wider digits save a pass). Any pointer may be NULL. */
+sf_status sf_get_tuning(const sf_handle* h, int32_t* block_sizes_out, int32_t* lanes_out, int32_t* sort_items_out,
+                        int32_t* sort_digit_bits_out);
 
 /* Text of the last error on this handle (or of the last failed create when h is NULL). */
 const char* sf_last_error_string(const sf_handle* h);

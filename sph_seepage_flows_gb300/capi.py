@@ -81,7 +81,7 @@ def load(path: str = LIB_PATH):
         "sf_launch_count": (i32, [H, P(i64)]),
         "sf_set_tuning": (i32, [H, i32, i32]),
         "sf_set_lanes": (i32, [H, i32]),
-        "sf_get_tuning": (i32, [H, P(i32), P(i32), P(i32)]),
+        "sf_get_tuning": (i32, [H, P(i32), P(i32), P(i32), P(i32)]),
         "sf_autotune": (i32, [H, f32, P(i32), P(i32)]),
         "sf_last_error_string": (ctypes.c_char_p, [H]),
         "sf_adjoint_run": (i32, [H, f32, i64, i64, P(f32), P(f32), P(f32), P(f32), P(f32), P(f32)]),
@@ -266,11 +266,12 @@ class Simulation:
         return {"block_sizes": dict(zip(names, list(bs))), "list_capacity": cap.value, **self.tuning()}
 
     def tuning(self) -> dict:
-        """sf_get_tuning: threads per particle of the neighbour passes and keys
-        per thread of the sort tiles currently in use."""
-        lanes, items = ctypes.c_int32(), ctypes.c_int32()
-        self._check(self.lib.sf_get_tuning(self.h, None, ctypes.byref(lanes), ctypes.byref(items)))
-        return {"lanes": lanes.value, "sort_items": items.value}
+        """sf_get_tuning: threads per particle of the neighbour passes, keys per
+        thread of the sort tiles and bits per radix digit currently in use."""
+        lanes, items, digit = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        self._check(self.lib.sf_get_tuning(self.h, None, ctypes.byref(lanes), ctypes.byref(items),
+                                           ctypes.byref(digit)))
+        return {"lanes": lanes.value, "sort_items": items.value, "sort_digit_bits": digit.value}
 
     # -------------------------------------------------------------- adjoint
     def adjoint(self, dt: float, n_substeps: int, target, checkpoint_every: int | None = None,

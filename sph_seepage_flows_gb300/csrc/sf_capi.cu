@@ -610,9 +610,12 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
         h->lanes = lanesForSlots(h->totalSlots, sms);
     }
     h->sc.tiles = sortTiles(h->totalSlots, h->sc.items);
-    // room for the smallest tiles, so that the tuner can change the tile size
-    SF_ALLOC(h->sc.hist, sizeof(unsigned) * 256 * size_t(sortTiles(h->totalSlots, 1)));
-    SF_ALLOC(h->sc.digitTotal, sizeof(unsigned) * 256);
+    // digits of 8 bits, or 9-11 when that saves a pass; room for the widest
+    // digits and the smallest tiles, so that the tuner can change both
+    h->sc.digitBits = sortDigitBits(h->sortBits);
+    const int maxRadix = 1 << std::max(8, h->sc.digitBits);
+    SF_ALLOC(h->sc.hist, sizeof(unsigned) * size_t(maxRadix) * size_t(sortTiles(h->totalSlots, 1)));
+    SF_ALLOC(h->sc.digitTotal, sizeof(unsigned) * size_t(maxRadix));
     SF_ALLOC(h->cs, sizeof(unsigned) * (size_t(h->totalCells) + 1));
     SF_ALLOC(h->bcs, sizeof(unsigned) * (size_t(h->totalCells) + 1));
     SF_ALLOC(h->bpos, sizeof(float4) * std::max<size_t>(1, size_t(h->totalB)));
@@ -1307,21 +1310,29 @@ sf_status sf_autotune(sf_handle* h, float dt, int32_t* block_sizes_out, int32_t*
             return SF_ERR_CUDA;
         return SF_OK;
     };
-    // sort tile size: sorting the sorted state again is the identity
+    // sort tile size and digit width: sorting the sorted state again is the identity
     {
         float best = 0.f;
-        int bestItems = h->sc.items;
-        for (int items : {8, 4, 2, 1}) {
-            h->sc.items = items;
-            h->sc.tiles = sortTiles(h->totalSlots, items);
-            float ms = 0.f;
-            if ((st = timed([&] { return runSort(h); }, ms))) break;
-            if (best == 0.f || ms < best) {
-                best = ms;
-                bestItems = items;
+        int bestItems = h->sc.items, bestDigit = h->sc.digitBits;
+        const int wide = sortDigitBits(h->sortBits);
+        for (int digit : {8, wide}) {
+            for (int items : {8, 4, 2, 1}) {
+                if (st) break;
+                h->sc.items = items;
+                h->sc.digitBits = digit;
+                h->sc.tiles = sortTiles(h->totalSlots, items);
+                float ms = 0.f;
+                if ((st = timed([&] { return runSort(h); }, ms))) break;
+                if (best == 0.f || ms < best) {
+                    best = ms;
+                    bestItems = items;
+                    bestDigit = digit;
+                }
             }
+            if (wide == 8) break;
         }
         h->sc.items = bestItems;
+        h->sc.digitBits = bestDigit;
         h->sc.tiles = sortTiles(h->totalSlots, bestItems);
     }
     // lanes per particle and the block size of every neighbour pass: every
@@ -1373,12 +1384,14 @@ sf_status sf_autotune(sf_handle* h, float dt, int32_t* block_sizes_out, int32_t*
     return SF_OK;
 }
 
-sf_status sf_get_tuning(const sf_handle* h, int32_t* block_sizes_out, int32_t* lanes_out, int32_t* sort_items_out) {
+sf_status sf_get_tuning(const sf_handle* h, int32_t* block_sizes_out, int32_t* lanes_out, int32_t* sort_items_out,
+                        int32_t* sort_digit_bits_out) {
     if (!h) return SF_ERR_INVALID;
     if (block_sizes_out)
         for (int k = 0; k < kTunedPasses; ++k) block_sizes_out[k] = h->block[k];
     if (lanes_out) *lanes_out = h->lanes;
     if (sort_items_out) *sort_items_out = h->sc.items ? h->sc.items : 8;
+    if (sort_digit_bits_out) *sort_digit_bits_out = h->sc.digitBits ? h->sc.digitBits : 8;
     return SF_OK;
 }
 

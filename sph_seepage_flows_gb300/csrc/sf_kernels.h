@@ -117,7 +117,11 @@ struct SortScratch {
     unsigned int* digitTotal;  // 256
     int tiles;               // sortTiles(n, items)
     int items;               // keys per thread of a tile: 1, 2, 4 or 8 (0 means 8)
+    int digitBits;           // 8-11 (0 means 8); hist holds 2^digitBits * tiles, digitTotal 2^digitBits
 };
+// Digit width for keys of keyBits bits: 8, or the narrowest of 9-11 that
+// needs fewer passes than 8-bit digits.
+int sortDigitBits(int keyBits);
 // Tiles of 256 threads x items keys over n keys.
 int sortTiles(int n, int items = 8);
 // Keys per thread for n keys: the largest of 8, 4, 2 that still gives every

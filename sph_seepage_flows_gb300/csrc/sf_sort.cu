@@ -9,10 +9,12 @@
 // cellStart[c] is the lower bound of c in the sorted keys. The result is the
 // same permutation and the same table as the reference's.
 //
-// Per 8-bit digit pass: kHist (per-tile digit counts), kScanTiles (per digit,
-// exclusive scan over tiles) and kScatter (digit offsets, in-tile stable rank:
-// rounds of 256 keys in index order, warp match for the rank inside a warp,
-// shared per-warp digit counts for the rank across warps).
+// Per digit pass (8-bit digits, or 9-11 bits when that saves a pass): kHist
+// (per-tile digit counts), kScanTiles (per digit, exclusive scan over tiles)
+// and kScatter (digit offsets, in-tile stable rank: rounds of 256 keys in
+// index order, warp match for the rank inside a warp, shared per-warp digit
+// counts for the rank across warps, moved into the running digit offsets by
+// the warp leaders of each round).
 #include "sf_kernels.h"
 
 namespace sfg {
@@ -27,21 +29,27 @@ int sortItemsFor(int n, int smCount) {
     return 1;
 }
 
-template <int kSortItems>
+template <int kSortItems, int kBits>
 __global__ void __launch_bounds__(kSortThreads) kHist(const unsigned int* __restrict__ keys, int n, int shift,
                                                       unsigned int* __restrict__ hist, int tiles) {
     constexpr int kTile = kSortThreads * kSortItems;
-    __shared__ unsigned int h[256];
-    h[threadIdx.x] = 0;
+    constexpr int R = 1 << kBits, kPer = R / kSortThreads;
+    __shared__ unsigned int h[R];
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) h[threadIdx.x * kPer + q] = 0;
     __syncthreads();
     const int base = blockIdx.x * kTile;
 #pragma unroll 4
     for (int r = 0; r < kSortItems; ++r) {
         const int idx = base + r * kSortThreads + threadIdx.x;
-        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
+        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & unsigned(R - 1)], 1u);
     }
     __syncthreads();
-    hist[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) {
+        const int d = threadIdx.x * kPer + q;
+        hist[size_t(d) * tiles + blockIdx.x] = h[d];
+    }
 }
 
 // Per-digit exclusive scan over tiles: block d scans hist[d * tiles ..
@@ -69,7 +77,7 @@ __global__ void __launch_bounds__(kSortThreads) kScanTiles(unsigned int* __restr
     if (threadIdx.x == 0) digitTotal[blockIdx.x] = carry;
 }
 
-template <int kSortItems>
+template <int kSortItems, int kBits>
 __global__ void __launch_bounds__(kSortThreads) kScatter(const unsigned int* __restrict__ keysIn,
                                                          const unsigned int* __restrict__ valsIn,
                                                          unsigned int* __restrict__ keysOut,
@@ -78,40 +86,55 @@ __global__ void __launch_bounds__(kSortThreads) kScatter(const unsigned int* __r
                                                          const unsigned int* __restrict__ digitTotal) {
     constexpr int kWarps = kSortThreads / 32;
     constexpr int kTile = kSortThreads * kSortItems;
-    __shared__ unsigned int base[256];
-    __shared__ unsigned int running[256];
-    __shared__ unsigned int cnt[kWarps][256];
+    constexpr int R = 1 << kBits, kPer = R / kSortThreads;
+    __shared__ unsigned int base[R];
+    __shared__ unsigned int running[R];
+    __shared__ unsigned char cnt[kWarps][R];  // keys of a digit per warp in one round (<= 32)
+    __shared__ unsigned int warpSum[kWarps];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    // digit offsets: exclusive scan of the digit totals
-    const unsigned int tot0 = digitTotal[tid];
-    running[tid] = tot0;
-    __syncthreads();
-    for (int o = 1; o < 256; o <<= 1) {
-        const unsigned int u = tid >= o ? running[tid - o] : 0u;
-        __syncthreads();
-        running[tid] += u;
-        __syncthreads();
-    }
-    base[tid] = running[tid] - tot0 + hist[tid * tiles + blockIdx.x];
-    __syncthreads();
-    running[tid] = 0;
+    // digit offsets: exclusive scan of the digit totals (kPer consecutive
+    // digits per thread, then a block scan of the threads' sums)
+    unsigned int tot[kPer], sum = 0;
 #pragma unroll
-    for (int w = 0; w < kWarps; ++w) cnt[w][tid] = 0;
+    for (int q = 0; q < kPer; ++q) {
+        tot[q] = digitTotal[tid * kPer + q];
+        sum += tot[q];
+    }
+    unsigned int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned int u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    if (lane == 31) warpSum[warp] = incl;
+    __syncthreads();
+    unsigned int acc = incl - sum;
+    for (int w = 0; w < warp; ++w) acc += warpSum[w];
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) {
+        const int d = tid * kPer + q;
+        base[d] = acc + hist[size_t(d) * tiles + blockIdx.x];
+        acc += tot[q];
+        running[d] = 0;
+    }
+    unsigned int* cnt32 = reinterpret_cast<unsigned int*>(&cnt[0][0]);
+    for (int q = tid; q < kWarps * R / 4; q += kSortThreads) cnt32[q] = 0u;
     __syncthreads();
     const unsigned int ltMask = (1u << lane) - 1u;
     const int tileBase = blockIdx.x * kTile;
     for (int r = 0; r < kSortItems; ++r) {
         const int idx = tileBase + r * kSortThreads + tid;
         const bool valid = idx < n;
-        unsigned int k = 0, v = 0, d = 256u;
+        unsigned int k = 0, v = 0, d = unsigned(R);
         if (valid) {
             k = keysIn[idx];
             v = valsIn ? valsIn[idx] : unsigned(idx);
-            d = (k >> shift) & 255u;
+            d = (k >> shift) & unsigned(R - 1);
         }
         const unsigned int peers = __match_any_sync(0xffffffffu, d);
         const unsigned int rank = __popc(peers & ltMask);
-        if (valid && rank == 0) cnt[warp][d] = __popc(peers);
+        const bool leader = valid && rank == 0;
+        if (leader) cnt[warp][d] = (unsigned char)__popc(peers);
         __syncthreads();
         if (valid) {
             unsigned int pre = 0;
@@ -121,42 +144,58 @@ __global__ void __launch_bounds__(kSortThreads) kScatter(const unsigned int* __r
             valsOut[pos] = v;
         }
         __syncthreads();
-        unsigned int tot = 0;
-#pragma unroll
-        for (int w = 0; w < kWarps; ++w) {
-            tot += cnt[w][tid];
-            cnt[w][tid] = 0;
+        // only the digits of this round: the warp leaders move their counts
+        if (leader) {
+            atomicAdd(&running[d], unsigned(__popc(peers)));
+            cnt[warp][d] = 0;
         }
-        running[tid] += tot;
         __syncthreads();
     }
 }
 
-template <int kSortItems>
-static void launchPass(cudaStream_t s, int n, int shift, const unsigned int* kIn, const unsigned int* vIn,
-                       unsigned int* kOut, unsigned int* vOut, const SortScratch& sc) {
+template <int kSortItems, int kBits>
+static void launchPassT(cudaStream_t s, int n, int shift, const unsigned int* kIn, const unsigned int* vIn,
+                        unsigned int* kOut, unsigned int* vOut, const SortScratch& sc) {
     const int tiles = sc.tiles;
-    kHist<kSortItems><<<tiles, kSortThreads, 0, s>>>(kIn, n, shift, sc.hist, tiles);
-    kScanTiles<<<256, kSortThreads, 0, s>>>(sc.hist, tiles, sc.digitTotal);
-    kScatter<kSortItems><<<tiles, kSortThreads, 0, s>>>(kIn, vIn, kOut, vOut, n, shift, sc.hist, tiles,
-                                                        sc.digitTotal);
+    kHist<kSortItems, kBits><<<tiles, kSortThreads, 0, s>>>(kIn, n, shift, sc.hist, tiles);
+    kScanTiles<<<1 << kBits, kSortThreads, 0, s>>>(sc.hist, tiles, sc.digitTotal);
+    kScatter<kSortItems, kBits><<<tiles, kSortThreads, 0, s>>>(kIn, vIn, kOut, vOut, n, shift, sc.hist, tiles,
+                                                               sc.digitTotal);
+}
+
+template <int kSortItems>
+static void launchPass(cudaStream_t s, int n, int shift, int bits, const unsigned int* kIn,
+                       const unsigned int* vIn, unsigned int* kOut, unsigned int* vOut, const SortScratch& sc) {
+    switch (bits) {
+    case 9: launchPassT<kSortItems, 9>(s, n, shift, kIn, vIn, kOut, vOut, sc); break;
+    case 10: launchPassT<kSortItems, 10>(s, n, shift, kIn, vIn, kOut, vOut, sc); break;
+    case 11: launchPassT<kSortItems, 11>(s, n, shift, kIn, vIn, kOut, vOut, sc); break;
+    default: launchPassT<kSortItems, 8>(s, n, shift, kIn, vIn, kOut, vOut, sc); break;
+    }
+}
+
+int sortDigitBits(int keyBits) {
+    const int passes8 = (keyBits + 7) / 8, passes11 = (keyBits + 10) / 11;
+    if (passes11 >= passes8) return 8;
+    return (keyBits + passes11 - 1) / passes11;  // the narrowest digits for that many passes
 }
 
 int radixSort(cudaStream_t s, int n, int bits, unsigned int* keys, SortScratch& sc, unsigned int** keysOut,
               unsigned int** permOut) {
-    const int passes = (bits + 7) / 8;
+    const int digit = sc.digitBits ? sc.digitBits : 8;
+    const int passes = (bits + digit - 1) / digit;
     unsigned int* kIn = keys;
     unsigned int* kOut = sc.keysAlt;
     unsigned int* vIn = nullptr;
     unsigned int* vOut = sc.vals;
     int launches = 0;
     for (int p = 0; p < passes; ++p) {
-        const int shift = 8 * p;
+        const int shift = digit * p;
         switch (sc.items) {
-        case 1: launchPass<1>(s, n, shift, kIn, vIn, kOut, vOut, sc); break;
-        case 2: launchPass<2>(s, n, shift, kIn, vIn, kOut, vOut, sc); break;
-        case 4: launchPass<4>(s, n, shift, kIn, vIn, kOut, vOut, sc); break;
-        default: launchPass<8>(s, n, shift, kIn, vIn, kOut, vOut, sc); break;
+        case 1: launchPass<1>(s, n, shift, digit, kIn, vIn, kOut, vOut, sc); break;
+        case 2: launchPass<2>(s, n, shift, digit, kIn, vIn, kOut, vOut, sc); break;
+        case 4: launchPass<4>(s, n, shift, digit, kIn, vIn, kOut, vOut, sc); break;
+        default: launchPass<8>(s, n, shift, digit, kIn, vIn, kOut, vOut, sc); break;
         }
         launches += 3;
         // next pass reads what this one wrote

@@ -39,6 +39,7 @@ def test_block_size_does_not_change_results(cuda_lib, name):
     out, info = run(sc, lambda s, dt: s.autotune(dt))
     assert set(info["block_sizes"].values()) <= {64, 128, 256}
     assert info["lanes"] in (1, 2, 4, 8) and info["sort_items"] in (1, 2, 4, 8)
+    assert 8 <= info["sort_digit_bits"] <= 11
     # the tuner's block sizes and sort tiles change nothing; its lane count
     # regroups the momentum sums, so compare with a run at that lane count
     same_lanes, _ = run(sc, lambda s, dt: s.set_lanes(info["lanes"]))
