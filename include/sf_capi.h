@@ -26,6 +26,7 @@
  *   sf_create_batched    no reference counterpart (independent scenes in one launch)
  *   sf_adjoint_run       no reference counterpart (reverse-mode gradient of a trajectory loss)
  *   sf_autotune          no reference counterpart (list capacity and block sizes of the passes)
+ *   sf_get_list_capacity no reference counterpart (neighbour list capacity and its growth)
  *
  * Threading: handles are independent; one handle must not be used from two
  * host threads at once. All work is issued on the stream given at creation.
@@ -207,8 +208,11 @@ sf_status sf_get_params(const sf_handle* h, int32_t scene, sf_params* params);
  * (elapsed device time) may be NULL. */
 sf_status sf_step(sf_handle* h, float render_interval, int64_t* n_substeps_out, float* ms_out);
 
-/* n substeps of every scene at a fixed dt, with no host synchronisation
- * (replayed from a captured CUDA graph). */
+/* n substeps of every scene at a fixed dt, replayed from captured CUDA graphs.
+ * Calls of up to 256 substeps return without waiting for the GPU. Longer calls
+ * wait, after each block of 256 substeps, until the block before it has run
+ * (the GPU keeps the newer block queued), so that the neighbour lists can grow
+ * within the call (see sf_get_list_capacity). */
 sf_status sf_substeps_fixed(sf_handle* h, float dt, int64_t n);
 
 /* One frame of the reference adaptive loop: while remaining > 1e-6:
@@ -251,6 +255,16 @@ sf_status sf_synchronize(sf_handle* h);
 /* Number of kernel launches the handle has issued so far (graph replays count
  * every kernel node). */
 sf_status sf_launch_count(const sf_handle* h, int64_t* launches);
+
+/* Neighbour list capacity (entries per particle) and how many times the
+ * handle has grown it (no reference counterpart: the reference walks the 27
+ * cells in every pass). A density pass that finds a particle's list full
+ * records the particle's neighbour count; the particle's later passes walk the
+ * stencil instead (same results, slower). sf_step, sf_substeps_fixed and
+ * sf_adjoint_run read those records once the GPU has reached them and
+ * re-allocate the lists for the largest count + 25% + 8, a multiple of 32 up
+ * to 256. Any pointer may be NULL. */
+sf_status sf_get_list_capacity(const sf_handle* h, int32_t* capacity, int64_t* growths);
 
 /* Launch configuration of the passes: threads per block (32, 64, 128 or 256)
  * for every tuned pass, and the particles each thread handles (1); 0 keeps a

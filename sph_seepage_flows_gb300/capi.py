@@ -79,6 +79,7 @@ def load(path: str = LIB_PATH):
         "sf_check_error": (i32, [H, P(ctypes.c_uint32)]),
         "sf_synchronize": (i32, [H]),
         "sf_launch_count": (i32, [H, P(i64)]),
+        "sf_get_list_capacity": (i32, [H, P(i32), P(i64)]),
         "sf_set_tuning": (i32, [H, i32, i32]),
         "sf_set_lanes": (i32, [H, i32]),
         "sf_get_tuning": (i32, [H, P(i32), P(i32), P(i32), P(i32)]),
@@ -204,6 +205,12 @@ class Simulation:
         v = ctypes.c_int64()
         self._check(self.lib.sf_launch_count(self.h, ctypes.byref(v)))
         return v.value
+
+    def list_capacity(self) -> tuple:
+        """sf_get_list_capacity: (neighbour list capacity, times the handle grew it)."""
+        cap, growths = ctypes.c_int32(), ctypes.c_int64()
+        self._check(self.lib.sf_get_list_capacity(self.h, ctypes.byref(cap), ctypes.byref(growths)))
+        return cap.value, growths.value
 
     def check_error(self) -> int:
         v = ctypes.c_uint32()

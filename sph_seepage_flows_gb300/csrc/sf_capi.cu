@@ -210,6 +210,12 @@ struct sf_handle {
     GraphCache graph[2];   // two-substep graphs, by starting buffer set
     GraphCache graph1[2];  // one-substep graphs, by starting buffer set
     int nbrCap = kMinNbr;                 // particle neighbour list capacity (per slot)
+    // list growth: copies of the scene states queued behind the substeps and
+    // read once they have landed (pinned, n_scenes each; two in flight at most)
+    SceneState* stateHost[2] = {nullptr, nullptr};
+    cudaEvent_t stateEvent[2] = {nullptr, nullptr};
+    bool statePending[2] = {false, false};
+    int64_t listGrowths = 0;
     int block[kTunedPasses] = {kSlotAlign, kSlotAlign, kSlotAlign, kSlotAlign, kSlotAlign, kSlotAlign};
     int lanes = 1;  // threads per slot of the momentum passes and the adjoint pair kernels
     unsigned int* dProbe = nullptr;       // neighbour-count probe word
@@ -319,6 +325,10 @@ struct sf_handle {
         for (auto& g : graph1)
             if (g.exec) cudaGraphExecDestroy(g.exec);
         devFree(dProbe);
+        for (int k = 0; k < 2; ++k) {
+            if (stateHost[k]) cudaFreeHost(stateHost[k]);
+            if (stateEvent[k]) cudaEventDestroy(stateEvent[k]);
+        }
         for (int k = 0; k < 2; ++k) {
             devFree(pos[k]);
             devFree(vel[k]);
@@ -439,13 +449,10 @@ sf_status countNeighborsMax(sf_handle* h, unsigned* maxCount) {
     return SF_OK;
 }
 
-// (Re)allocates the particle lists for the capacity the current state needs.
-sf_status probeListCapacity(sf_handle* h) {
-    unsigned mx = 0;
-    sf_status st = countNeighborsMax(h, &mx);
-    if (st) return st;
-    const int cap = capacityFor(mx);
-    if (h->nbr && cap == h->nbrCap) return SF_OK;
+// Re-allocates the particle lists with `cap` entries per slot. The captured
+// graphs hold the old lists and are dropped; the scenes' overflow records
+// and the state copies in flight describe the old capacity and are cleared.
+sf_status resizeLists(sf_handle* h, int cap) {
     if (h->nbr && h->cuda(cudaStreamSynchronize(h->stream), "sync before list realloc")) return SF_ERR_CUDA;
     devFree(h->nbr);
     if (h->cuda(cudaMalloc(reinterpret_cast<void**>(&h->nbr), sizeof(unsigned) * size_t(h->totalSlots) * cap),
@@ -453,9 +460,60 @@ sf_status probeListCapacity(sf_handle* h) {
         h->cuda(cudaMemsetAsync(h->nbr, 0, sizeof(unsigned) * size_t(h->totalSlots) * cap, h->stream),
                 "cudaMemset neighbour lists"))
         return SF_ERR_CUDA;
+    for (int s = 0; s < h->nScenes; ++s)
+        if (h->cuda(cudaMemsetAsync(&h->dState[s].list_need, 0, sizeof(unsigned), h->stream), "clear list_need"))
+            return SF_ERR_CUDA;
+    h->statePending[0] = h->statePending[1] = false;
     h->nbrCap = cap;
     h->dropGraphs();
     return SF_OK;
+}
+
+// (Re)allocates the particle lists for the capacity the current state needs.
+sf_status probeListCapacity(sf_handle* h) {
+    unsigned mx = 0;
+    sf_status st = countNeighborsMax(h, &mx);
+    if (st) return st;
+    const int cap = capacityFor(mx);
+    if (h->nbr && cap == h->nbrCap) return SF_OK;
+    return resizeLists(h, cap);
+}
+
+// Queues a copy of the scene states behind the work queued so far, into a
+// free copy slot; returns the slot, or -1 when both copies are still in flight.
+int queueStateCopy(sf_handle* h) {
+    for (int k = 0; k < 2; ++k) {
+        if (h->statePending[k]) continue;
+        if (cudaMemcpyAsync(h->stateHost[k], h->dState, sizeof(SceneState) * size_t(h->nScenes),
+                            cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+            cudaEventRecord(h->stateEvent[k], h->stream) != cudaSuccess) {
+            cudaGetLastError();
+            return -1;
+        }
+        h->statePending[k] = true;
+        return k;
+    }
+    return -1;
+}
+
+// Reads the state copies that have landed (waiting for copy slot `waitSlot`,
+// if >= 0) and grows the particle lists when a density pass found a list
+// full: the new capacity holds the largest count reported plus the usual
+// headroom (at most kMaxNbr). The substeps in between walked the stencil for
+// the particles concerned, which gives the same results more slowly.
+sf_status growListsIfFull(sf_handle* h, int waitSlot) {
+    unsigned need = 0;
+    for (int k = 0; k < 2; ++k) {
+        if (!h->statePending[k]) continue;
+        const cudaError_t e = k == waitSlot ? cudaEventSynchronize(h->stateEvent[k]) : cudaEventQuery(h->stateEvent[k]);
+        if (e == cudaErrorNotReady) continue;
+        if (h->cuda(e, "state copy")) return SF_ERR_CUDA;
+        h->statePending[k] = false;
+        for (int s = 0; s < h->nScenes; ++s) need = std::max(need, h->stateHost[k][s].list_need);
+    }
+    if (need == 0 || capacityFor(need) <= h->nbrCap) return SF_OK;
+    ++h->listGrowths;
+    return resizeLists(h, capacityFor(need));
 }
 
 bool validScene(const sf_params* p, const sf_boundary_params* b, const sf_scene_init* in, int64_t cap,
@@ -626,6 +684,11 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
     SF_ALLOC(h->dErr, sizeof(unsigned));
     SF_ALLOC(h->dProbe, sizeof(unsigned));
 #undef SF_ALLOC
+    for (int k = 0; k < 2; ++k)
+        if (h->cuda(cudaMallocHost(reinterpret_cast<void**>(&h->stateHost[k]), sizeof(SceneState) * n_scenes),
+                    "cudaMallocHost state copy") ||
+            h->cuda(cudaEventCreateWithFlags(&h->stateEvent[k], cudaEventDisableTiming), "state copy event"))
+            return bail(SF_ERR_CUDA);
     // host staging of the initial state
     std::vector<float4> hpos(M, make_float4(0, 0, 0, 0)), hvel(M, make_float4(0, 0, 0, 0)),
         hcol(M, make_float4(0, 0, 0, 0)), hmat(M, make_float4(0, 0, 0, 0));
@@ -748,6 +811,7 @@ sf_status sf_run_stage(sf_handle* h, int32_t stage, float time_arg, int32_t adap
 
 sf_status sf_step(sf_handle* h, float render_interval, int64_t* n_substeps_out, float* ms_out) {
     if (!h) return SF_ERR_INVALID;
+    if (sf_status gs = growListsIfFull(h, -1)) return gs;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (ms_out) {
         cudaEventCreate(&e0);
@@ -756,6 +820,7 @@ sf_status sf_step(sf_handle* h, float render_interval, int64_t* n_substeps_out, 
     }
     sf_status st = runSubstep(h, render_interval, 1);
     if (st != SF_OK) return st;
+    queueStateCopy(h);
     if (ms_out) {
         cudaEventRecord(e1, h->stream);
         cudaEventSynchronize(e1);
@@ -822,9 +887,10 @@ static sf_status ensureGraph(sf_handle* h, GraphCache& g, int nsub, float dt) {
     return SF_OK;
 }
 
-sf_status sf_substeps_fixed(sf_handle* h, float dt, int64_t n) {
-    if (!h || n < 0) return SF_ERR_INVALID;
-    if (n == 0) return SF_OK;
+namespace {
+
+// n fixed-dt substeps replayed from the captured graphs.
+sf_status queueSubstepsFixed(sf_handle* h, float dt, int64_t n) {
     sf_status st = SF_OK;
     if (n % 2 == 1) {  // the odd substep from a one-substep graph of this buffer set
         GraphCache& g1 = h->graph1[h->cur];
@@ -842,6 +908,33 @@ sf_status sf_substeps_fixed(sf_handle* h, float dt, int64_t n) {
         }
     }
     h->sorted = true;
+    return SF_OK;
+}
+
+// Substeps between list checks in a long call.
+constexpr int64_t kListCheckEvery = 256;
+
+}  // namespace
+
+// A call queues its substeps without waiting for them, except in long calls:
+// there, after each block of kListCheckEvery substeps, the host waits until
+// the block before it has run (the GPU keeps the newer block queued) and
+// grows the lists if one was found full.
+sf_status sf_substeps_fixed(sf_handle* h, float dt, int64_t n) {
+    if (!h || n < 0) return SF_ERR_INVALID;
+    if (n == 0) return SF_OK;
+    sf_status st = growListsIfFull(h, n > kListCheckEvery ? 0 : -1);
+    if (st == SF_OK && n > kListCheckEvery) st = growListsIfFull(h, 1);
+    if (st) return st;
+    int prevSlot = -1;
+    for (int64_t done = 0; done < n;) {
+        const int64_t m = std::min(kListCheckEvery, n - done);
+        if ((st = queueSubstepsFixed(h, dt, m))) return st;
+        done += m;
+        const int slot = queueStateCopy(h);
+        if (done < n && prevSlot >= 0 && (st = growListsIfFull(h, prevSlot))) return st;
+        prevSlot = slot;
+    }
     return SF_OK;
 }
 
@@ -1251,6 +1344,13 @@ sf_status sf_synchronize(sf_handle* h) {
     return h->cuda(cudaStreamSynchronize(h->stream), "sf_synchronize");
 }
 
+sf_status sf_get_list_capacity(const sf_handle* h, int32_t* capacity, int64_t* growths) {
+    if (!h) return SF_ERR_INVALID;
+    if (capacity) *capacity = h->nbrCap;
+    if (growths) *growths = h->listGrowths;
+    return SF_OK;
+}
+
 sf_status sf_launch_count(const sf_handle* h, int64_t* launches) {
     if (!h || !launches) return SF_ERR_INVALID;
     *launches = h->launches;
@@ -1656,6 +1756,8 @@ sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t che
     const int64_t T = n_substeps, K = std::min(checkpoint_every, n_substeps);
     const int64_t nSeg = (T + K - 1) / K;
     const int64_t lastLen = T - (nSeg - 1) * K;
+    // lists found full by earlier calls grow first (the stored substeps are sized by the capacity)
+    if (sf_status gs = growListsIfFull(h, -1)) return gs;
     // snapshots: segment starts [0, nSeg - 1) and the final state; slabs: one segment
     if (ensureAdjoint(h, size_t(nSeg), size_t(K))) return SF_ERR_CUDA;
     const size_t sStride = snapStride(h);
@@ -1765,6 +1867,7 @@ sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t che
         cudaEventElapsedTime(&ms_out[0], ev[0], ev[1]);
         cudaEventElapsedTime(&ms_out[1], ev[1], ev[2]);
     }
+    queueStateCopy(h);
     return h->cuda(cudaGetLastError(), "sf_adjoint_run");
 }
 

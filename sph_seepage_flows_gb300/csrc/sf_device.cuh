@@ -79,7 +79,7 @@ struct SceneState {
     int n;                   // live particle count
     long long n_sub;         // sub-step count of the last integrate
     float dt;                // dt of the last integrate
-    float pad;
+    unsigned int list_need;  // largest neighbour count that found its list full (0: none)
 };
 
 // ---------------------------------------------------------------- float3 math

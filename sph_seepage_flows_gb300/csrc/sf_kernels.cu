@@ -293,6 +293,9 @@ __global__ void __launch_bounds__(kSlotAlign, 6) kDensity(const SceneDev* __rest
     L.cnt[slot] = unsigned(min(cS, 0xFFFF)) | (unsigned(min(cW, 0xFFFF)) << 16);
     L.bcnt[slot] = bc;
     L.ccnt[slot] = cc;
+    // a full list asks the host to grow the capacity; until then the passes
+    // walk the stencil for this particle (same results, slower)
+    if (!listed) atomicMax(&state[sid].list_need, unsigned(cS + cW));
     float density, pressure = 0.f;
     if (!water) {
         density = S.rho1;
@@ -510,6 +513,9 @@ __global__ void __launch_bounds__(kSlotAlign) kDensityLanes(const SceneDev* __re
     L.cnt[slot] = unsigned(min(cS, 0xFFFF)) | (unsigned(min(cW, 0xFFFF)) << 16);
     L.bcnt[slot] = bc;
     L.ccnt[slot] = cc;
+    // a full list asks the host to grow the capacity; until then the passes
+    // walk the stencil for this particle (same results, slower)
+    if (!listed) atomicMax(&state[sid].list_need, unsigned(cS + cW));
     float pressure = 0.f;
     if (water) {
         if (S.tait) {
