@@ -192,6 +192,8 @@ struct sf_handle {
     // per-substep arrays
     float4 *aux = nullptr, *flow = nullptr, *adh = nullptr, *avgadh = nullptr, *drag = nullptr, *acc = nullptr;
     float2* dp = nullptr;
+    float2* vrec2 = nullptr;  // gather records, rewritten every substep
+    float4* grec4 = nullptr;
     unsigned int *keys = nullptr, *cs = nullptr, *bcs = nullptr;
     unsigned int* nbrCnt = nullptr;
     int* bnbrCnt = nullptr;
@@ -293,6 +295,8 @@ struct sf_handle {
         b.mat4 = mat[cur];
         b.bpos4 = bpos;
         b.dp = dp;
+        b.vrec2 = vrec2;
+        b.grec4 = grec4;
         return b;
     }
     // Drop the captured substep graphs (after a change of buffers or launch shapes).
@@ -344,6 +348,8 @@ struct sf_handle {
         devFree(drag);
         devFree(acc);
         devFree(dp);
+        devFree(vrec2);
+        devFree(grec4);
         devFree(keys);
         devFree(nbrCnt);
         devFree(bnbrCnt);
@@ -650,6 +656,8 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
     SF_ALLOC(h->drag, F4);
     SF_ALLOC(h->acc, F4);
     SF_ALLOC(h->dp, sizeof(float2) * M);
+    SF_ALLOC(h->vrec2, sizeof(float2) * M);
+    SF_ALLOC(h->grec4, sizeof(float4) * M);
     SF_ALLOC(h->keys, sizeof(unsigned) * M);
     SF_ALLOC(h->nbrCnt, sizeof(unsigned) * M);
     SF_ALLOC(h->bnbrCnt, sizeof(int) * M);
@@ -988,10 +996,35 @@ __global__ void kGetField(int field, int n, int slotOff, int cellOff, int order,
     }
 }
 
+// The values the passes derive from a slot's fields for later passes (the
+// w components, the water (D, P) pair and the gather records), recomputed
+// with the passes' operations after a field was set, so that running the
+// later stages gives the same results as after the passes themselves.
+__device__ void refreshDerived(int s, const float4* pos, const float4* vel, const float4* aux, float4* flow,
+                               float4* avgadh, float4* drag, float2* dp, float2* vrec2, float4* grec4,
+                               const SceneDev& S) {
+    const float4 p = pos[s], v = vel[s], a = aux[s];
+    if (p.w < 0.f) {
+        const float bz = bezier(S.adhG, a.z);
+        flow[s].w = bz;
+        drag[s].w = v.w;
+        vrec2[s] = make_float2(bz, -p.w / v.w);
+        grec4[s] = make_float4(v.x, v.y, v.z, a.z);
+    } else if (p.w > 0.f) {
+        const float vol = p.w / v.w;
+        vrec2[s] = make_float2(a.y * vol, vol);
+        const float D = v.w / fmaxf(kEps, a.w);
+        const float P = a.x / fmaxf(kEps, D * D);
+        dp[s] = make_float2(D, P);
+        avgadh[s].w = D;
+        grec4[s] = make_float4(v.x, v.y, v.z, P);
+    }
+}
+
 __global__ void kSetField(int field, int n, int slotOff, int order, float4* pos, float4* vel, float4* col,
                           float4* mat, float2* amc, const int* __restrict__ pid, float4* aux, float4* flow,
-                          float4* adh, float4* avgadh, float4* drag, float4* acc, const void* in,
-                          const SceneDev* __restrict__ scene) {
+                          float4* adh, float4* avgadh, float4* drag, float4* acc, float2* dp, float2* vrec2,
+                          float4* grec4, const void* in, const SceneDev* __restrict__ scene) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int s = slotOff + i;
@@ -1017,16 +1050,10 @@ __global__ void kSetField(int field, int n, int slotOff, int order, float4* pos,
     }
     case SF_FIELD_RADIUS: mat[s].w = f[o]; break;
     case SF_FIELD_MASS: pos[s].w = pos[s].w < 0.f ? -f[o] : f[o]; break;
-    case SF_FIELD_DENSITY:  // sand: also the copy the water momentum pass gathers with the drag
-        vel[s].w = f[o];
-        if (pos[s].w < 0.f) drag[s].w = f[o];
-        break;
+    case SF_FIELD_DENSITY: vel[s].w = f[o]; break;
     case SF_FIELD_PRESSURE: aux[s].x = f[o]; break;
     case SF_FIELD_VOIDAGE: aux[s].w = f[o]; aux[s].y = f[o]; break;
-    case SF_FIELD_SATURATION:  // and the adhesion factor the average-flow pass derives from it
-        aux[s].z = f[o];
-        if (pos[s].w < 0.f) flow[s].w = bezier(scene->adhG, f[o]);
-        break;
+    case SF_FIELD_SATURATION: aux[s].z = f[o]; break;
     case SF_FIELD_MAX_SATURATION: col[s].w = f[o]; break;
     case SF_FIELD_AVG_FLOW: set3(flow); break;
     case SF_FIELD_AVG_DRAG: set3(drag); break;
@@ -1034,6 +1061,13 @@ __global__ void kSetField(int field, int n, int slotOff, int order, float4* pos,
     case SF_FIELD_AVG_ADHESION: set3(avgadh); break;
     case SF_FIELD_CDA0ASAT: set3(mat); break;
     case SF_FIELD_AMCAMCP: amc[s] = make_float2(f[2 * o], f[2 * o + 1]); break;
+    default: break;
+    }
+    switch (field) {
+    case SF_FIELD_VEL: case SF_FIELD_LABEL: case SF_FIELD_MASS: case SF_FIELD_DENSITY: case SF_FIELD_PRESSURE:
+    case SF_FIELD_VOIDAGE: case SF_FIELD_SATURATION:
+        refreshDerived(s, pos, vel, aux, flow, avgadh, drag, dp, vrec2, grec4, *scene);
+        break;
     default: break;
     }
 }
@@ -1077,7 +1111,7 @@ __global__ void __launch_bounds__(kVecParticles) kGetVec3(int n, int slotOff, co
     if (t < rem) reinterpret_cast<float*>(o + words)[t] = buf[4 * words + t];
 }
 __global__ void __launch_bounds__(kVecParticles) kSetVec3(int n, int slotOff, float4* __restrict__ dst,
-                                                          const float4* __restrict__ in) {
+                                                          const float4* __restrict__ in, float4* __restrict__ rec) {
     __shared__ float4 buf4[kVecParticles * 3 / 4];
     float* buf = reinterpret_cast<float*>(buf4);
     const int t = threadIdx.x, p0 = blockIdx.x * kVecParticles, cnt = min(kVecParticles, n - p0);
@@ -1092,6 +1126,13 @@ __global__ void __launch_bounds__(kVecParticles) kSetVec3(int n, int slotOff, fl
         v.y = buf[3 * t + 1];
         v.z = buf[3 * t + 2];
         dst[slotOff + p0 + t] = v;
+        if (rec) {  // velocities: the copy in the gather records
+            float4 r = rec[slotOff + p0 + t];
+            r.x = v.x;
+            r.y = v.y;
+            r.z = v.z;
+            rec[slotOff + p0 + t] = r;
+        }
     }
 }
 
@@ -1230,12 +1271,12 @@ sf_status sf_set_field(sf_handle* h, int32_t scene, int32_t field, int32_t order
     float4* vec = order == SF_ORDER_SORTED ? vec3Array(h, field) : nullptr;
     if (vec && (reinterpret_cast<uintptr_t>(from) & 15u) == 0)
         kSetVec3<<<int((n + kVecParticles - 1) / kVecParticles), kVecParticles, 0, h->stream>>>(
-            int(n), S.slot_off, vec, static_cast<const float4*>(from));
+            int(n), S.slot_off, vec, static_cast<const float4*>(from), field == SF_FIELD_VEL ? h->grec4 : nullptr);
     else
         kSetField<<<int((n + 255) / 256), 256, 0, h->stream>>>(field, int(n), S.slot_off, order, h->pos[c],
                                                                h->vel[c], h->col[c], h->mat[c], h->amc[c], h->pid[c],
                                                                h->aux, h->flow, h->adh, h->avgadh, h->drag, h->acc,
-                                                               from, h->dScenes + scene);
+                                                               h->dp, h->vrec2, h->grec4, from, h->dScenes + scene);
     if (h->cuda(cudaGetLastError(), "set_field launch")) return SF_ERR_CUDA;
     if (!src_on_device) return h->cuda(cudaStreamSynchronize(h->stream), "set_field sync");
     return SF_OK;

@@ -542,7 +542,8 @@ __global__ void __launch_bounds__(kSlotAlign) kAvgFlow(const SceneDev* __restric
                                                        const int* __restrict__ blockScene, NbrLists L,
                                                        const float4* __restrict__ pos4,
                                                        const float4* __restrict__ vel4, float4* __restrict__ aux4,
-                                                       float4* __restrict__ flow4) {
+                                                       float4* __restrict__ flow4, float2* __restrict__ vrec2,
+                                                       float4* __restrict__ grec4) {
     SF_SLOT_PROLOGUE_G
     const float4 pi4 = pos4[slot];
     if (pi4.w == 0.f) return;
@@ -611,12 +612,22 @@ __global__ void __launch_bounds__(kSlotAlign) kAvgFlow(const SceneDev* __restric
         avg = mk3(0.f, 0.f, 0.f);
     // w: the adhesion Bezier factor of a sand particle's saturation, which
     // every water neighbour's adhesion term uses (computed once here)
-    flow4[slot] = make_float4(avg.x, avg.y, avg.z, sandI ? bezier(S.adhG, v_s) : 0.f);
+    const float bz = sandI ? bezier(S.adhG, v_s) : 0.f;
+    flow4[slot] = make_float4(avg.x, avg.y, avg.z, bz);
     float4 a = aux4[slot];
     a.y = 1.f - sand_volume;
     a.z = v_s;
     a.w = a.y;  // the reference's voidage array holds the fluid voidage until the sand pass
     aux4[slot] = a;
+    // the records the later passes gather (the same products their terms form)
+    const float4 vi4 = vel4[slot];
+    if (sandI) {
+        vrec2[slot] = make_float2(bz, -pi4.w / vi4.w);
+        grec4[slot] = make_float4(vi4.x, vi4.y, vi4.z, v_s);
+    } else {
+        const float vol = pi4.w / vi4.w;
+        vrec2[slot] = make_float2(a.y * vol, vol);
+    }
 }
 
 // ------------------------------------------------ voidage / adhesion stage
@@ -630,7 +641,8 @@ __global__ void __launch_bounds__(kSlotAlign) kVoidageAdhesion(
     const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene, NbrLists L,
     const float4* __restrict__ pos4, const float4* __restrict__ vel4, float4* __restrict__ aux4,
     const float4* __restrict__ flow4, float4* __restrict__ adh4, float4* __restrict__ avgadh4,
-    float4* __restrict__ col4, float2* __restrict__ dp) {
+    float4* __restrict__ col4, float2* __restrict__ dp, const float2* __restrict__ vrec2,
+    float4* __restrict__ grec4) {
     SF_SLOT_PROLOGUE_G
     const float4 pi4 = pos4[slot];
     if (pi4.w == 0.f) return;
@@ -642,12 +654,12 @@ __global__ void __launch_bounds__(kSlotAlign) kVoidageAdhesion(
             S, L, slot, pi, pos4, part,
             [&](int j) {
                 const float4 pj = pos4[j];
+                const float2 r = vrec2[j];  // (fluid voidage x volume, volume)
                 const float3 dij = pi - xyz(pj);
-                const float vj = pj.w / vel4[j].w;
                 const float wij = poly6(S, len3(dij));
                 Terms<2> t;
-                t.v[0] = aux4[j].y * vj * wij;
-                t.v[1] = vj * wij;
+                t.v[0] = r.x * wij;
+                t.v[1] = r.y * wij;
                 return t;
             },
             [&](const Terms<2>& t) {
@@ -676,13 +688,14 @@ __global__ void __launch_bounds__(kSlotAlign) kVoidageAdhesion(
             S, L, slot, pi, pos4, part,
             [&](int j) {
                 const float4 pj = pos4[j];
+                const float2 r = vrec2[j];  // (adhesion Bezier factor of sat_j, volume)
                 const float3 dpij = pi - xyz(pj);
                 const float ldp = len3(dpij);
                 const float wij = poly6(S, ldp);
                 const float adij = adhesionSpline(S, ldp);
                 const float mj = -pj.w;
-                const float3 a = flow4[j].w * mi * mj * adij * dpij / fmaxf(kEps, ldp);  // w: bezier(adhG, sat_j)
-                const float vj = mj / vel4[j].w;
+                const float3 a = r.x * mi * mj * adij * dpij / fmaxf(kEps, ldp);
+                const float vj = r.y;
                 Terms<4> t;
                 t.v[0] = a.x;
                 t.v[1] = a.y;
@@ -697,12 +710,15 @@ __global__ void __launch_bounds__(kSlotAlign) kVoidageAdhesion(
         if (part != 0) return;
         adh4[slot] = make_float4(ad.x, ad.y, ad.z, v_s);  // w: the average's denominator, for the adjoint
         const float3 avg = v_s != 0.f ? ad / v_s : mk3(0.f, 0.f, 0.f);
-        avgadh4[slot] = make_float4(avg.x, avg.y, avg.z, 0.f);
         // the effective density and pressure term, with the operations every
         // momentum pair term of this particle uses
         const float4 ai = aux4[slot];
-        const float D = vel4[slot].w / fmaxf(kEps, ai.w);
-        dp[slot] = make_float2(D, ai.x / fmaxf(kEps, D * D));
+        const float4 vi4 = vel4[slot];
+        const float D = vi4.w / fmaxf(kEps, ai.w);
+        const float P = ai.x / fmaxf(kEps, D * D);
+        dp[slot] = make_float2(D, P);
+        avgadh4[slot] = make_float4(avg.x, avg.y, avg.z, D);  // w: D, for the sand momentum pass
+        grec4[slot] = make_float4(vi4.x, vi4.y, vi4.z, P);
     }
 }
 
@@ -720,8 +736,8 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kSandMomentum(
     const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene, NbrLists L,
     const float4* __restrict__ pos4, const float4* __restrict__ vel4, const float4* __restrict__ aux4,
     const float4* __restrict__ flow4, const float4* __restrict__ avgadh4, const float4* __restrict__ mat4,
-    const float4* __restrict__ bpos4, float2* __restrict__ dp, float4* __restrict__ drag4,
-    float4* __restrict__ acc4) {
+    const float4* __restrict__ bpos4, float2* __restrict__ dp, const float4* __restrict__ grec4,
+    float4* __restrict__ drag4, float4* __restrict__ acc4) {
     SF_SLOT_PROLOGUE_G
     const float4 pi4 = pos4[slot];
     if (!(pi4.w < 0.f)) {
@@ -741,8 +757,9 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kSandMomentum(
     // iterate the contact list (or the sand list when it overflowed)
     auto contact = [&](int j) {
         const float3 dij = xyz(pos4[j]) - pi;
-        f += demForce(dij, xyz(vel4[j]) - vi, S.rij2, S.kn, S.ks, S.tan2);
-        f += capillaryForce(S, dij, (ai.z + aux4[j].z) / 2.f);
+        const float4 gj = grec4[j];  // (velocity, saturation)
+        f += demForce(dij, xyz(gj) - vi, S.rij2, S.kn, S.ks, S.tan2);
+        f += capillaryForce(S, dij, (ai.z + gj.w) / 2.f);
     };
     const int cc = L.ccnt[slot];
     if (cc <= kMaxContact) {
@@ -760,13 +777,14 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kSandMomentum(
         const float4 pj = pos4[j];
         const float3 dij = pi - xyz(pj);
         const float4 aj = aux4[j];
+        const float4 gj = avgadh4[j];  // (average adhesion, D)
         const float wij = poly6(S, len3(dij));
         if (aj.w > 0.f && aj.w <= 1.f) {
-            const float dj = dp[j].x;
+            const float dj = gj.w;
             v_w += pj.w / dj * wij;
             f += -mi * pj.w * aj.x / fmaxf(kEps, di * dj) * spikyGrad(S, dij);
         }
-        f += wij * vol_i * xyz(avgadh4[j]);
+        f += wij * vol_i * xyz(gj);
     }, part);
     if (S.shape_boundary) {
         forBoundaryNeighbors<G>(S, L, slot, pi, bpos4, [&](int b) {
@@ -817,7 +835,8 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kWaterMomentum(
     const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene, SceneState* __restrict__ state,
     NbrLists L, const float4* __restrict__ pos4, const float4* __restrict__ vel4, const float4* __restrict__ aux4,
     const float4* __restrict__ drag4, const float4* __restrict__ adh4, const float4* __restrict__ bpos4,
-    const float2* __restrict__ dp, float4* __restrict__ acc4, unsigned int* errWord) {
+    const float2* __restrict__ dp, const float4* __restrict__ grec4, float4* __restrict__ acc4,
+    unsigned int* errWord) {
     SF_SLOT_PROLOGUE_G
     const float4 pi4 = pos4[slot];
     float alen = 0.f;
@@ -834,13 +853,12 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kWaterMomentum(
             if (j == slot) return;
             const float4 pj = pos4[j];
             const float3 dij = pi - xyz(pj);
-            const float2 dpj = dp[j];
-            const float4 vj4 = vel4[j];
-            const float dj = dpj.x;
+            const float4 gj = grec4[j];  // (velocity, P)
             const float3 nab = spikyGrad(S, dij);
-            a += -pj.w * (pterm_i + dpj.y) * nab;
-            const float dd = dot3(vi - xyz(vj4), dij);
+            a += -pj.w * (pterm_i + gj.w) * nab;
+            const float dd = dot3(vi - xyz(gj), dij);
             if (dd < 0.f) {
+                const float dj = dp[j].x;
                 const float pij = -S.nu / (di + dj) * (dd / (dot3(dij, dij) + kEps));
                 a += -pj.w * pij * nab;
             }
@@ -1043,8 +1061,8 @@ void launchDensity(const LaunchCtx& c, const PassBuffers& b) {
 }
 
 template <int G> void launchAvgFlowG(const LaunchCtx& c, const PassBuffers& b) {
-    kAvgFlow<G><<<grid(c, kPassAvgFlow) * G, c.block[kPassAvgFlow], 0, c.stream>>>(c.scenes, c.blockScene, b.lists,
-                                                                                  b.pos4, b.vel4, b.aux4, b.flow4);
+    kAvgFlow<G><<<grid(c, kPassAvgFlow) * G, c.block[kPassAvgFlow], 0, c.stream>>>(
+        c.scenes, c.blockScene, b.lists, b.pos4, b.vel4, b.aux4, b.flow4, b.vrec2, b.grec4);
 }
 void launchAvgFlow(const LaunchCtx& c, const PassBuffers& b) {
     switch (c.lanes) {
@@ -1057,7 +1075,8 @@ void launchAvgFlow(const LaunchCtx& c, const PassBuffers& b) {
 
 template <int G> void launchVoidageAdhesionG(const LaunchCtx& c, const PassBuffers& b) {
     kVoidageAdhesion<G><<<grid(c, kPassVoidage) * G, c.block[kPassVoidage], 0, c.stream>>>(
-        c.scenes, c.blockScene, b.lists, b.pos4, b.vel4, b.aux4, b.flow4, b.adh4, b.avgadh4, b.col4, b.dp);
+        c.scenes, c.blockScene, b.lists, b.pos4, b.vel4, b.aux4, b.flow4, b.adh4, b.avgadh4, b.col4, b.dp, b.vrec2,
+        b.grec4);
 }
 void launchVoidageAdhesion(const LaunchCtx& c, const PassBuffers& b) {
     switch (c.lanes) {
@@ -1070,8 +1089,8 @@ void launchVoidageAdhesion(const LaunchCtx& c, const PassBuffers& b) {
 
 template <int G> void launchSandMomentumG(const LaunchCtx& c, const PassBuffers& b) {
     kSandMomentum<G><<<grid(c, kPassSand) * G, c.block[kPassSand], 0, c.stream>>>(
-        c.scenes, c.blockScene, b.lists, b.pos4, b.vel4, b.aux4, b.flow4, b.avgadh4, b.mat4, b.bpos4, b.dp, b.drag4,
-        b.acc4);
+        c.scenes, c.blockScene, b.lists, b.pos4, b.vel4, b.aux4, b.flow4, b.avgadh4, b.mat4, b.bpos4, b.dp, b.grec4,
+        b.drag4, b.acc4);
 }
 void launchSandMomentum(const LaunchCtx& c, const PassBuffers& b) {
     switch (c.lanes) {
@@ -1084,8 +1103,8 @@ void launchSandMomentum(const LaunchCtx& c, const PassBuffers& b) {
 
 template <int G> void launchWaterMomentumG(const LaunchCtx& c, const PassBuffers& b) {
     kWaterMomentum<G><<<grid(c, kPassWater) * G, c.block[kPassWater], 0, c.stream>>>(
-        c.scenes, c.blockScene, c.state, b.lists, b.pos4, b.vel4, b.aux4, b.drag4, b.adh4, b.bpos4, b.dp, b.acc4,
-        c.errWord);
+        c.scenes, c.blockScene, c.state, b.lists, b.pos4, b.vel4, b.aux4, b.drag4, b.adh4, b.bpos4, b.dp, b.grec4,
+        b.acc4, c.errWord);
 }
 void launchWaterMomentum(const LaunchCtx& c, const PassBuffers& b) {
     switch (c.lanes) {

@@ -87,6 +87,18 @@ struct PassBuffers {
     // instead of summing them again. adh4.w of water holds the denominator
     // of its average adhesion for the same reason.
     float2* dp;
+    // Gather records, rewritten every substep so that a neighbour term loads
+    // one record besides the neighbour's position (values bit-identical to
+    // the ones the terms used to gather from several arrays):
+    //   vrec2, average-flow pass -> voidage / adhesion pass: water (fluid
+    //     voidage x volume m / rho, volume), sand (adhesion Bezier factor of
+    //     its saturation, volume);
+    //   grec4: sand (velocity, saturation) from the average-flow pass, for the
+    //     DEM contacts; water (velocity, pressure term P) from the voidage /
+    //     adhesion pass, for the water momentum pairs.
+    // avgadh4.w of water holds its effective density D for the sand momentum pass.
+    float2* vrec2;
+    float4* grec4;
 };
 
 // Threads per slot of the lane-split passes (momentum passes and the adjoint
