@@ -385,19 +385,20 @@ struct sf_handle {
 
 namespace {
 
-// The sort stage: keys, stable radix sort, cell table, reorder into the other buffer set.
+// The sort stage: keys (with the first radix pass's tile histograms), stable
+// radix sort, reorder into the other buffer set (with the cell table).
 sf_status runSort(sf_handle* h) {
     LaunchCtx c = h->ctx();
-    launchKeys(c, h->pos[h->cur], h->keys);
+    launchKeysHist(c, h->totalSlots, h->pos[h->cur], h->keys, h->sc);
     unsigned int* perm = nullptr;
-    int l = radixSort(h->stream, h->totalSlots, h->sortBits, h->keys, h->sc, &h->sortedKeys, &perm);
-    launchCellStart(h->stream, h->totalSlots, h->totalCells, h->sortedKeys, h->cs);
+    int l = radixSort(h->stream, h->totalSlots, h->sortBits, h->keys, h->sc, &h->sortedKeys, &perm, true);
     const int o = h->cur, t = 1 - h->cur;
     launchReorder(h->stream, h->totalSlots, perm, h->pos[o], h->vel[o], h->col[o], h->mat[o], h->amc[o], h->pid[o],
-                  h->pos[t], h->vel[t], h->col[t], h->mat[t], h->amc[t], h->pid[t]);
+                  h->pos[t], h->vel[t], h->col[t], h->mat[t], h->amc[t], h->pid[t], h->sortedKeys, h->totalCells,
+                  h->cs);
     h->cur = t;
     h->sorted = true;
-    h->launches += 3 + l;
+    h->launches += 2 + l;
     return h->cuda(cudaGetLastError(), "sort stage launch");
 }
 

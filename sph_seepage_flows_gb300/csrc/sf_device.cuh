@@ -112,6 +112,16 @@ __device__ __forceinline__ int3 cellOf(const SceneDev& S, float3 p) {
 }
 __device__ __forceinline__ int localHash(const SceneDev& S, int3 c) { return c.x * S.gy * S.gz + c.y * S.gz + c.z; }
 
+// Pos2GridHash (helper_thrust.cuh:66-89) into the global cell space; parking
+// slots (w = 0) get the scene's parking cell. A non-finite position sets bit 0
+// of the error word.
+__device__ __forceinline__ unsigned int slotKey(const SceneDev& S, float4 p, unsigned int* errWord) {
+    if (p.w == 0.f) return unsigned(S.cell_off + S.ncell);
+    const float3 q = make_float3(p.x, p.y, p.z);
+    if (!(isfinite(q.x) && isfinite(q.y) && isfinite(q.z))) atomicOr(errWord, 1u);
+    return unsigned(S.cell_off + localHash(S, cellOf(S, q)));
+}
+
 // Poly6Kernel::operator() (cuda_sph_kernel.cuh:90-97)
 __device__ __forceinline__ float poly6(const SceneDev& S, float r) {
     float r2 = r * r;

@@ -50,24 +50,6 @@ namespace sfg {
     const int sid = blockScene[(blockIdx.x * (blockDim.x / G)) / kSlotAlign];   \
     const SceneDev& S = scenes[sid];
 
-// ---------------------------------------------------------------------- keys
-// Pos2GridHash (helper_thrust.cuh:66-89) into the global cell space; parking
-// slots get the scene's parking cell.
-__global__ void kKeys(const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene,
-                      const float4* __restrict__ pos4, unsigned int* __restrict__ keys, unsigned int* errWord) {
-    SF_SLOT_PROLOGUE
-    const float4 p = pos4[slot];
-    unsigned int k;
-    if (p.w == 0.f) {
-        k = unsigned(S.cell_off + S.ncell);
-    } else {
-        const float3 q = xyz(p);
-        if (!(isfinite(q.x) && isfinite(q.y) && isfinite(q.z))) atomicOr(errWord, 1u);
-        k = unsigned(S.cell_off + localHash(S, cellOf(S, q)));
-    }
-    keys[slot] = k;
-}
-
 // ----------------------------------------------------------- boundary volume
 // ComputeBoundaryVolume_CUDA (cuda_sph_system_gpu.cuh:19-67): V_b = 1 / max(sum_{j != i} W, eps).
 __global__ void kBoundaryVolume(const SceneDev* __restrict__ scenes, int sid, float4* __restrict__ bpos4,
@@ -1031,10 +1013,6 @@ static inline int grid(const LaunchCtx& c, int pass) { return c.slotBlocks * (kS
 
 void launchNeighborCountMax(const LaunchCtx& c, const float4* pos4, const unsigned int* cs, unsigned int* maxCount) {
     kNeighborCountMax<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, pos4, cs, maxCount);
-}
-
-void launchKeys(const LaunchCtx& c, const float4* pos4, unsigned int* keys) {
-    kKeys<<<c.slotBlocks, kSlotAlign, 0, c.stream>>>(c.scenes, c.blockScene, pos4, keys, c.errWord);
 }
 
 void launchBoundaryVolume(const LaunchCtx& c, int sid, int nb, float4* bpos4, const int* blabel,

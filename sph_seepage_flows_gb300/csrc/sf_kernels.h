@@ -106,7 +106,6 @@ struct PassBuffers {
 // to 8, while fewer than 2048 threads per SM would run.
 int lanesForSlots(long long totalSlots, int smCount);
 
-void launchKeys(const LaunchCtx& c, const float4* pos4, unsigned int* keys);
 void launchBoundaryVolume(const LaunchCtx& c, int sid, int nb, float4* bpos4, const int* blabel,
                           const unsigned int* bcs);
 void launchDensity(const LaunchCtx& c, const PassBuffers& b);
@@ -142,14 +141,22 @@ int sortTiles(int n, int items = 8);
 int sortItemsFor(int n, int smCount);
 // Sorts keys[0..n) (only the low `bits` bits are examined) and writes the
 // stable permutation to *permOut (new index -> old index) and the sorted keys
-// to *keysOut; both point into keys/scratch buffers. Returns kernels launched.
+// to *keysOut; both point into keys/scratch buffers. firstHistDone: sc.hist
+// already holds the first digit's tile histograms (launchKeysHist). Returns
+// kernels launched.
 int radixSort(cudaStream_t s, int n, int bits, unsigned int* keys, SortScratch& sc, unsigned int** keysOut,
-              unsigned int** permOut);
+              unsigned int** permOut, bool firstHistDone = false);
+// The cell key of every slot of the handle (n slots, a multiple of 256) and
+// the first radix pass's tile histograms into sc.hist, in one launch.
+void launchKeysHist(const LaunchCtx& c, int n, const float4* pos4, unsigned int* keys, const SortScratch& sc);
 // cellStart[c] = first index i with sortedKeys[i] >= c, for c in [0, nCells]
 void launchCellStart(cudaStream_t s, int n, int nCells, const unsigned int* sortedKeys, unsigned int* cellStart);
-// Gather the persistent per-slot arrays into sorted order.
+// Gather the persistent per-slot arrays into sorted order (n a multiple of
+// 32) and write the cell table cellStart of the sorted keys (as
+// launchCellStart) in the same launch.
 void launchReorder(cudaStream_t s, int n, const unsigned int* perm, const float4* pos, const float4* vel,
                    const float4* col, const float4* mat, const float2* amc, const int* pid, float4* posOut,
-                   float4* velOut, float4* colOut, float4* matOut, float2* amcOut, int* pidOut);
+                   float4* velOut, float4* colOut, float4* matOut, float2* amcOut, int* pidOut,
+                   const unsigned int* sortedKeys, int nCells, unsigned int* cellStart);
 
 }  // namespace sfg

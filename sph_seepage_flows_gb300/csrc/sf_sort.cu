@@ -14,7 +14,11 @@
 // and kScatter (digit offsets, in-tile stable rank: rounds of 256 keys in
 // index order, warp match for the rank inside a warp, shared per-warp digit
 // counts for the rank across warps, moved into the running digit offsets by
-// the warp leaders of each round).
+// the warp leaders of each round). The first pass takes its tile histograms
+// from the key kernel (kKeysHist), and the reorder writes the cell table
+// (cellStart[c] = lower bound of c) as it gathers, so a sort stage of two
+// digit passes is six launches.
+#include "sf_device.cuh"
 #include "sf_kernels.h"
 
 namespace sfg {
@@ -49,6 +53,71 @@ __global__ void __launch_bounds__(kSortThreads) kHist(const unsigned int* __rest
     for (int q = 0; q < kPer; ++q) {
         const int d = threadIdx.x * kPer + q;
         hist[size_t(d) * tiles + blockIdx.x] = h[d];
+    }
+}
+
+// The cell keys (slotKey) of one tile of slots and the tile's histogram of
+// their first digit: kHist of the first pass fused into the key computation.
+// Rounds of 256 slots are 256-slot blocks of one scene each.
+template <int kSortItems, int kBits>
+__global__ void __launch_bounds__(kSortThreads) kKeysHist(const SceneDev* __restrict__ scenes,
+                                                          const int* __restrict__ blockScene,
+                                                          const float4* __restrict__ pos4,
+                                                          unsigned int* __restrict__ keys, unsigned int* errWord,
+                                                          int n, unsigned int* __restrict__ hist, int tiles) {
+    constexpr int kTile = kSortThreads * kSortItems;
+    constexpr int R = 1 << kBits, kPer = R / kSortThreads;
+    __shared__ unsigned int h[R];
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) h[threadIdx.x * kPer + q] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * kTile;
+#pragma unroll 4
+    for (int r = 0; r < kSortItems; ++r) {
+        const int slot = base + r * kSortThreads + threadIdx.x;
+        if (slot < n) {
+            const unsigned int k = slotKey(scenes[blockScene[slot / kSlotAlign]], pos4[slot], errWord);
+            keys[slot] = k;
+            atomicAdd(&h[k & unsigned(R - 1)], 1u);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) {
+        const int d = threadIdx.x * kPer + q;
+        hist[size_t(d) * tiles + blockIdx.x] = h[d];
+    }
+}
+
+template <int kSortItems>
+static void launchKeysHistI(const LaunchCtx& c, int n, const float4* pos4, unsigned int* keys,
+                            const SortScratch& sc) {
+    switch (sc.digitBits) {
+    case 9:
+        kKeysHist<kSortItems, 9><<<sc.tiles, kSortThreads, 0, c.stream>>>(c.scenes, c.blockScene, pos4, keys,
+                                                                          c.errWord, n, sc.hist, sc.tiles);
+        break;
+    case 10:
+        kKeysHist<kSortItems, 10><<<sc.tiles, kSortThreads, 0, c.stream>>>(c.scenes, c.blockScene, pos4, keys,
+                                                                           c.errWord, n, sc.hist, sc.tiles);
+        break;
+    case 11:
+        kKeysHist<kSortItems, 11><<<sc.tiles, kSortThreads, 0, c.stream>>>(c.scenes, c.blockScene, pos4, keys,
+                                                                           c.errWord, n, sc.hist, sc.tiles);
+        break;
+    default:
+        kKeysHist<kSortItems, 8><<<sc.tiles, kSortThreads, 0, c.stream>>>(c.scenes, c.blockScene, pos4, keys,
+                                                                          c.errWord, n, sc.hist, sc.tiles);
+        break;
+    }
+}
+
+void launchKeysHist(const LaunchCtx& c, int n, const float4* pos4, unsigned int* keys, const SortScratch& sc) {
+    switch (sc.items) {
+    case 1: launchKeysHistI<1>(c, n, pos4, keys, sc); break;
+    case 2: launchKeysHistI<2>(c, n, pos4, keys, sc); break;
+    case 4: launchKeysHistI<4>(c, n, pos4, keys, sc); break;
+    default: launchKeysHistI<8>(c, n, pos4, keys, sc); break;
     }
 }
 
@@ -155,9 +224,9 @@ __global__ void __launch_bounds__(kSortThreads) kScatter(const unsigned int* __r
 
 template <int kSortItems, int kBits>
 static void launchPassT(cudaStream_t s, int n, int shift, const unsigned int* kIn, const unsigned int* vIn,
-                        unsigned int* kOut, unsigned int* vOut, const SortScratch& sc) {
+                        unsigned int* kOut, unsigned int* vOut, const SortScratch& sc, bool histDone) {
     const int tiles = sc.tiles;
-    kHist<kSortItems, kBits><<<tiles, kSortThreads, 0, s>>>(kIn, n, shift, sc.hist, tiles);
+    if (!histDone) kHist<kSortItems, kBits><<<tiles, kSortThreads, 0, s>>>(kIn, n, shift, sc.hist, tiles);
     kScanTiles<<<1 << kBits, kSortThreads, 0, s>>>(sc.hist, tiles, sc.digitTotal);
     kScatter<kSortItems, kBits><<<tiles, kSortThreads, 0, s>>>(kIn, vIn, kOut, vOut, n, shift, sc.hist, tiles,
                                                                sc.digitTotal);
@@ -165,12 +234,13 @@ static void launchPassT(cudaStream_t s, int n, int shift, const unsigned int* kI
 
 template <int kSortItems>
 static void launchPass(cudaStream_t s, int n, int shift, int bits, const unsigned int* kIn,
-                       const unsigned int* vIn, unsigned int* kOut, unsigned int* vOut, const SortScratch& sc) {
+                       const unsigned int* vIn, unsigned int* kOut, unsigned int* vOut, const SortScratch& sc,
+                       bool histDone) {
     switch (bits) {
-    case 9: launchPassT<kSortItems, 9>(s, n, shift, kIn, vIn, kOut, vOut, sc); break;
-    case 10: launchPassT<kSortItems, 10>(s, n, shift, kIn, vIn, kOut, vOut, sc); break;
-    case 11: launchPassT<kSortItems, 11>(s, n, shift, kIn, vIn, kOut, vOut, sc); break;
-    default: launchPassT<kSortItems, 8>(s, n, shift, kIn, vIn, kOut, vOut, sc); break;
+    case 9: launchPassT<kSortItems, 9>(s, n, shift, kIn, vIn, kOut, vOut, sc, histDone); break;
+    case 10: launchPassT<kSortItems, 10>(s, n, shift, kIn, vIn, kOut, vOut, sc, histDone); break;
+    case 11: launchPassT<kSortItems, 11>(s, n, shift, kIn, vIn, kOut, vOut, sc, histDone); break;
+    default: launchPassT<kSortItems, 8>(s, n, shift, kIn, vIn, kOut, vOut, sc, histDone); break;
     }
 }
 
@@ -181,7 +251,7 @@ int sortDigitBits(int keyBits) {
 }
 
 int radixSort(cudaStream_t s, int n, int bits, unsigned int* keys, SortScratch& sc, unsigned int** keysOut,
-              unsigned int** permOut) {
+              unsigned int** permOut, bool firstHistDone) {
     const int digit = sc.digitBits ? sc.digitBits : 8;
     const int passes = (bits + digit - 1) / digit;
     unsigned int* kIn = keys;
@@ -191,13 +261,14 @@ int radixSort(cudaStream_t s, int n, int bits, unsigned int* keys, SortScratch& 
     int launches = 0;
     for (int p = 0; p < passes; ++p) {
         const int shift = digit * p;
+        const bool histDone = p == 0 && firstHistDone;
         switch (sc.items) {
-        case 1: launchPass<1>(s, n, shift, digit, kIn, vIn, kOut, vOut, sc); break;
-        case 2: launchPass<2>(s, n, shift, digit, kIn, vIn, kOut, vOut, sc); break;
-        case 4: launchPass<4>(s, n, shift, digit, kIn, vIn, kOut, vOut, sc); break;
-        default: launchPass<8>(s, n, shift, digit, kIn, vIn, kOut, vOut, sc); break;
+        case 1: launchPass<1>(s, n, shift, digit, kIn, vIn, kOut, vOut, sc, histDone); break;
+        case 2: launchPass<2>(s, n, shift, digit, kIn, vIn, kOut, vOut, sc, histDone); break;
+        case 4: launchPass<4>(s, n, shift, digit, kIn, vIn, kOut, vOut, sc, histDone); break;
+        default: launchPass<8>(s, n, shift, digit, kIn, vIn, kOut, vOut, sc, histDone); break;
         }
-        launches += 3;
+        launches += histDone ? 2 : 3;
         // next pass reads what this one wrote
         unsigned int* t = kIn;
         kIn = kOut;
@@ -228,13 +299,40 @@ void launchCellStart(cudaStream_t s, int n, int nCells, const unsigned int* sort
     kCellStart<<<(nCells + 1 + 255) / 256, 256, 0, s>>>(n, nCells, sortedKeys, cellStart);
 }
 
+// cellStart[c] = v for c in [lo, hi), written by the lanes of one warp
+// (all 32 call it): short runs by their own lane, long runs (the empty cells
+// before a sparse region) by the whole warp, one run after the other.
+__device__ __forceinline__ void fillCellRuns(unsigned int* __restrict__ cs, unsigned int lo, unsigned int hi,
+                                             unsigned int v) {
+    constexpr unsigned int kShort = 8;
+    if (hi - lo <= kShort)
+        for (unsigned int c = lo; c < hi; ++c) cs[c] = v;
+    const unsigned int lane = threadIdx.x & 31u;
+    for (unsigned int longRuns = __ballot_sync(0xffffffffu, hi - lo > kShort); longRuns; longRuns &= longRuns - 1u) {
+        const int src = __ffs(longRuns) - 1;
+        const unsigned int l = __shfl_sync(0xffffffffu, lo, src), h = __shfl_sync(0xffffffffu, hi, src);
+        const unsigned int w = __shfl_sync(0xffffffffu, v, src);
+        for (unsigned int c = l + lane; c < h; c += 32u) cs[c] = w;
+    }
+}
+
 __global__ void kReorder(int n, const unsigned int* __restrict__ perm, const float4* __restrict__ pos,
                          const float4* __restrict__ vel, const float4* __restrict__ col,
                          const float4* __restrict__ mat, const float2* __restrict__ amc, const int* __restrict__ pid,
                          float4* __restrict__ posOut, float4* __restrict__ velOut, float4* __restrict__ colOut,
-                         float4* __restrict__ matOut, float2* __restrict__ amcOut, int* __restrict__ pidOut) {
+                         float4* __restrict__ matOut, float2* __restrict__ amcOut, int* __restrict__ pidOut,
+                         const unsigned int* __restrict__ sk, int nCells, unsigned int* __restrict__ cs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n) return;  // n is a multiple of 32: whole warps stay
+    // cell table (the lower bound of every cell in the sorted keys): index i
+    // starts the cells after its predecessor's key up to its own key; the
+    // last index also ends the table
+    // (keys above nCells, which only a corrupt position could give, are
+    // clamped: that leaves every lower bound in [0, nCells] unchanged)
+    const unsigned int top = unsigned(nCells);
+    const unsigned int k = min(sk[i], top);
+    fillCellRuns(cs, i == 0 ? 0u : min(sk[i - 1], top) + 1u, k + 1u, unsigned(i));
+    fillCellRuns(cs, k + 1u, i == n - 1 ? unsigned(nCells) + 1u : k + 1u, unsigned(n));
     const unsigned int o = perm[i];
     posOut[i] = pos[o];
     velOut[i] = vel[o];
@@ -246,9 +344,10 @@ __global__ void kReorder(int n, const unsigned int* __restrict__ perm, const flo
 
 void launchReorder(cudaStream_t s, int n, const unsigned int* perm, const float4* pos, const float4* vel,
                    const float4* col, const float4* mat, const float2* amc, const int* pid, float4* posOut,
-                   float4* velOut, float4* colOut, float4* matOut, float2* amcOut, int* pidOut) {
+                   float4* velOut, float4* colOut, float4* matOut, float2* amcOut, int* pidOut,
+                   const unsigned int* sortedKeys, int nCells, unsigned int* cellStart) {
     kReorder<<<(n + 255) / 256, 256, 0, s>>>(n, perm, pos, vel, col, mat, amc, pid, posOut, velOut, colOut, matOut,
-                                            amcOut, pidOut);
+                                            amcOut, pidOut, sortedKeys, nCells, cellStart);
 }
 
 }  // namespace sfg
