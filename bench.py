@@ -429,6 +429,7 @@ def run_ours(args, rank, world):
     nbrs = sim.field("neighbors").astype(np.int64) - 1
     lab = sim.field("label")
     pairs = int(4 * nbrs[lab == 0].sum() + 3 * nbrs[lab == 1].sum())
+    bgeo = None if args.no_bgeo else bgeo_export_timing(sim, n)
     batched = None if args.no_batched else batched_comparison(stream)
     adjoint = None if args.no_adjoint else adjoint_comparison(stream)
     calib = None if args.no_calibration else calibration_timing(stream)
@@ -459,12 +460,36 @@ def run_ours(args, rank, world):
         "device_error_flags": flags,
         "clocks": clk,
         "e2e": e2e,
+        "bgeo_export": bgeo,
         "cpu_baseline": cpu,
         "batched": batched,
         "adjoint": adjoint,
         "calibration": calib,
     }
     print(json.dumps(line), flush=True)
+
+
+def bgeo_export_timing(sim, n):
+    """sf_export_bgeo of the whole scene (the reference's per-frame export):
+    wall time per call, GPU packing, device-to-host copy and file write
+    included, into a RAM-backed folder where there is one."""
+    import shutil
+    import tempfile
+    base = "/dev/shm" if os.path.isdir("/dev/shm") else None
+    folder = tempfile.mkdtemp(prefix="sf_bgeo_", dir=base)
+    try:
+        sim.export_bgeo(folder, "warm")
+        reps = 3
+        t0 = time.perf_counter()
+        for k in range(reps):
+            sim.export_bgeo(folder, f"{k:04d}")
+        el = (time.perf_counter() - t0) / reps
+        size = os.path.getsize(os.path.join(folder, "0000.bgeo"))
+    finally:
+        shutil.rmtree(folder, ignore_errors=True)
+    return {"particles": n, "file_bytes": size, "ms_per_export": el * 1e3, "file_gb_per_s": size / el / 1e9,
+            "folder": "RAM-backed (/dev/shm)" if base else "temporary folder",
+            "path": "sf_export_bgeo: GPU big-endian packing + D2H to pinned memory + file write"}
 
 
 def main():
@@ -479,6 +504,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-calibration", action="store_true")
+    ap.add_argument("--no-bgeo", action="store_true")
     ap.add_argument("--adjoint-substeps", type=int, default=0,
                     help="only time the gradient run of the workload over this many substeps")
     ap.add_argument("--checkpoint-every", type=int, default=0,

@@ -20,6 +20,9 @@
  *   sf_frame_adaptive    the adaptive frame loop of seepage_flows/src/seepageflow/main.cpp:235-247
  *   sf_get_field         CudaSFParticles::Get*Ptr getters (include/kiri_pbs_cuda/particle/cuda_sf_particles.cuh:170-190)
  *   sf_get_cell_table    CudaGNBaseSearcher::GetCellStart / GetGridSize (include/kiri_pbs_cuda/searcher/cuda_neighbor_searcher.cuh:35-44)
+ *   sf_export_bgeo       ExportBgeoFileCUDA (seepage_flows/include/kiri_utils.h:364-448) with a handle's particle arrays
+ *   sf_export_bgeo_device ExportBgeoFileCUDA itself (device arrays in the reference's layout)
+ *   sf_read_bgeo         ReadBgeoFileForGPU (seepage_flows/include/kiri_utils.h:252-302)
  *   sf_add_sph_particles CudaSFParticles::AddSphParticles (src/kiri_pbs_cuda/particle/cuda_sf_particles.cu:50-68)
  *   sf_run_stage         the protected per-pass methods of CudaSphSFSolver (src/kiri_pbs_cuda/solver/seepage_flow/cuda_sph_sf_solver.cu:20-402)
  *   sf_substeps_fixed    fixed-substep mode of main.cpp:250-258 (no reference counterpart for the graph capture)
@@ -234,6 +237,29 @@ sf_status sf_set_field(sf_handle* h, int32_t scene, int32_t field, int32_t order
 /* Cell start table of one scene (which = 0 particles, 1 boundary), as
  * scene-relative offsets: G+1 entries, entry G = the scene's count. */
 sf_status sf_get_cell_table(sf_handle* h, int32_t scene, int32_t which, int64_t* dst, int64_t count);
+
+/* Houdini classic .bgeo files (the format the reference reads and writes
+ * through partio). The export writes folder_path/file_name.bgeo (creating
+ * the folder) with the point attributes position, Cd (float 3), pscale
+ * (float 1) and label (int 1), one point per particle:
+ *   sf_export_bgeo: one scene of a handle, in the current (cell-sorted)
+ *     order, as the reference exports its particle arrays after a frame;
+ *   sf_export_bgeo_device: n particles from device arrays in the reference's
+ *     layout (float3 positions and colours, float radii, size_t labels),
+ *     issued on `stream` (NULL: the default stream); errors go to
+ *     sf_last_error_string(NULL).
+ * The records are packed big-endian on the GPU; both calls return after the
+ * file is written. */
+sf_status sf_export_bgeo(sf_handle* h, int32_t scene, const char* folder_path, const char* file_name);
+sf_status sf_export_bgeo_device(const char* folder_path, const char* file_name, const float* pos3, const float* col3,
+                                const float* radius, const uint64_t* labels, int64_t n, void* stream);
+
+/* Reads the points of a .bgeo file as ReadBgeoFileForGPU does: 4 floats per
+ * point (x, y, z, pscale), pscale 0.01 when the file has no float pscale
+ * attribute, y and z swapped when flip_yz. Host only (no GPU work). With
+ * xyzs_out == NULL it only stores the point count in *n_out; otherwise
+ * capacity (points) must hold them all. Errors go to sf_last_error_string(NULL). */
+sf_status sf_read_bgeo(const char* path, int32_t flip_yz, float* xyzs_out, int64_t capacity, int64_t* n_out);
 sf_status sf_get_grid(const sf_handle* h, int32_t scene, int32_t grid_size[3], int64_t* n_cells);
 
 sf_status sf_size(const sf_handle* h, int32_t scene, int64_t* n, int64_t* capacity);

@@ -718,4 +718,54 @@ inline void CudaSFParticles::AddSphParticles(Vec_Float3 p, float3 col, float3 ve
     if (st == SF_ERR_CAPACITY) std::printf("Current SPH particles numbers exceed maximum particles. \n");
 }
 
+
+// ------------------------------------------------------------- bgeo files
+// ReadBgeoFileForGPU, ReadMultiBgeoFilesForGPU and ExportBgeoFileCUDA
+// (seepage_flows/include/kiri_utils.h:252-448), over sf_read_bgeo and
+// sf_export_bgeo_device. DB_PBR_PATH is the reference's asset root (a compile
+// definition there); the reader looks for DB_PBR_PATH "bgeo/<folder>/<name>.bgeo".
+#ifndef DB_PBR_PATH
+#define DB_PBR_PATH "./"
+#endif
+using String = std::string;
+using Vec_String = Vector<std::string>;
+
+inline String UInt2Str4Digit(unsigned int input) {  // frame names of the export (main.cpp:270)
+    char buf[16];
+    std::snprintf(buf, sizeof(buf), "%04u", input);
+    return String(buf);
+}
+
+inline Vec_Float4 ReadBgeoFileForGPU(String Folder, String Name, bool flip_yz = false) {
+    const String path = String(DB_PBR_PATH) + "bgeo/" + Folder + "/" + Name + ".bgeo";
+    Vec_Float4 out;
+    int64_t n = 0;
+    if (sf_read_bgeo(path.c_str(), flip_yz ? 1 : 0, nullptr, 0, &n) == SF_OK) {
+        out.resize(size_t(n));
+        if (n == 0 || sf_read_bgeo(path.c_str(), flip_yz ? 1 : 0, reinterpret_cast<float*>(out.data()), n, &n) == SF_OK)
+            return out;
+    }
+    std::fprintf(stderr, "%s\n", sf_last_error_string(nullptr));
+    return Vec_Float4();
+}
+
+inline Vec_Float4 ReadMultiBgeoFilesForGPU(Vec_String folders, Vec_String file_names, bool flip_yz = false) {
+    Vec_Float4 out;
+    for (size_t k = 0; k < folders.size() && k < file_names.size(); ++k) {
+        const Vec_Float4 one = ReadBgeoFileForGPU(folders[k], file_names[k], flip_yz);
+        out.insert(out.end(), one.begin(), one.end());
+    }
+    return out;
+}
+
+inline void ExportBgeoFileCUDA(const std::string& folder_path, const std::string& file_name, const float3* positions,
+                               const float3* colors, const float* radius, const size_t* labels,
+                               const size_t particles_num) {
+    static_assert(sizeof(size_t) == sizeof(uint64_t), "labels are read as 64-bit words");
+    if (sf_export_bgeo_device(folder_path.c_str(), file_name.c_str(), reinterpret_cast<const float*>(positions),
+                              reinterpret_cast<const float*>(colors), radius,
+                              reinterpret_cast<const uint64_t*>(labels), int64_t(particles_num), nullptr) != SF_OK)
+        std::fprintf(stderr, "%s\n", sf_last_error_string(nullptr));
+}
+
 }  // namespace KIRI

@@ -21,7 +21,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "libsf_gb300.so")
-SOURCES = ["sf_kernels.cu", "sf_sort.cu", "sf_adjoint.cu", "sf_capi.cu", "sf_noalloc.cu"]
+SOURCES = ["sf_kernels.cu", "sf_sort.cu", "sf_adjoint.cu", "sf_capi.cu", "sf_noalloc.cu", "sf_bgeo.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

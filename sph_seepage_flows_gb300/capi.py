@@ -88,6 +88,10 @@ def load(path: str = LIB_PATH):
         "sf_adjoint_run": (i32, [H, f32, i64, i64, P(f32), P(f32), P(f32), P(f32), P(f32), P(f32)]),
         "sf_cell_sort_noalloc": (i32, [P(SfBoundaryParams), ctypes.c_void_p, i64, ctypes.c_void_p, ctypes.c_void_p,
                                        H]),
+        "sf_export_bgeo": (i32, [H, i32, ctypes.c_char_p, ctypes.c_char_p]),
+        "sf_export_bgeo_device": (i32, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_void_p, i64, H]),
+        "sf_read_bgeo": (i32, [ctypes.c_char_p, i32, P(f32), i64, P(i64)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -99,6 +103,33 @@ def load(path: str = LIB_PATH):
 
 def device_count() -> int:
     return int(load().sf_device_count())
+
+
+def _global_error() -> str:
+    return (load().sf_last_error_string(None) or b"").decode()
+
+
+def read_bgeo(path: str, flip_yz: bool = False) -> np.ndarray:
+    """sf_read_bgeo (ReadBgeoFileForGPU): (n, 4) float32 of x, y, z, pscale."""
+    lib = load()
+    n = ctypes.c_int64()
+    if lib.sf_read_bgeo(path.encode(), int(flip_yz), None, 0, ctypes.byref(n)) != SF_OK:
+        raise RuntimeError(_global_error())
+    out = np.empty((n.value, 4), np.float32)
+    if lib.sf_read_bgeo(path.encode(), int(flip_yz), _fptr(out), n.value, ctypes.byref(n)) != SF_OK:
+        raise RuntimeError(_global_error())
+    return out
+
+
+def export_bgeo_device(folder: str, name: str, pos3_ptr: int, col3_ptr: int, radius_ptr: int, label_ptr: int,
+                       n: int, stream: int = 0):
+    """sf_export_bgeo_device (ExportBgeoFileCUDA): device pointers to float3
+    positions and colours, float radii and 64-bit labels of n particles."""
+    st = load().sf_export_bgeo_device(folder.encode(), name.encode(), ctypes.c_void_p(pos3_ptr),
+                                      ctypes.c_void_p(col3_ptr), ctypes.c_void_p(radius_ptr),
+                                      ctypes.c_void_p(label_ptr), int(n), ctypes.c_void_p(stream or None))
+    if st != SF_OK:
+        raise RuntimeError(_global_error())
 
 
 def _fptr(a):
@@ -205,6 +236,10 @@ class Simulation:
         v = ctypes.c_int64()
         self._check(self.lib.sf_launch_count(self.h, ctypes.byref(v)))
         return v.value
+
+    def export_bgeo(self, folder: str, name: str, scene: int = 0):
+        """sf_export_bgeo: folder/name.bgeo with position, Cd, pscale, label in the current order."""
+        self._check(self.lib.sf_export_bgeo(self.h, scene, folder.encode(), name.encode()))
 
     def list_capacity(self) -> tuple:
         """sf_get_list_capacity: (neighbour list capacity, times the handle grew it)."""

@@ -164,6 +164,11 @@ struct GraphCache {
 namespace sfg {
 // Error text of handle-less entry points (sf_last_error_string(NULL)).
 void setGlobalError(const std::string& msg) { g_createError = msg; }
+
+// sf_bgeo.cu: pinned host buffers and the .bgeo export of slots in the handle layout
+sf_status ensurePinned(void*& p, size_t& have, size_t bytes, std::string& err);
+sf_status exportBgeoSlots(cudaStream_t s, int64_t n, const float4* pos4, const float4* col4, const float4* mat4,
+                          void* dev, void* host, const char* folder, const char* name, std::string& err);
 }  // namespace sfg
 
 struct sf_handle {
@@ -207,6 +212,9 @@ struct sf_handle {
     // staging for field access
     void* stage = nullptr;
     size_t stageBytes = 0;
+    // pinned host buffer of the .bgeo export
+    void* exportHost = nullptr;
+    size_t exportHostBytes = 0;
     bool sorted = false;
     int64_t launches = 0;
     GraphCache graph[2];   // two-substep graphs, by starting buffer set
@@ -379,6 +387,7 @@ struct sf_handle {
         devFree(snap);
         devFree(slab);
         if (stage) cudaFree(stage);
+        if (exportHost) cudaFreeHost(exportHost);
         if (ownStream && stream) cudaStreamDestroy(stream);
     }
 };
@@ -1281,6 +1290,18 @@ sf_status sf_set_field(sf_handle* h, int32_t scene, int32_t field, int32_t order
     if (h->cuda(cudaGetLastError(), "set_field launch")) return SF_ERR_CUDA;
     if (!src_on_device) return h->cuda(cudaStreamSynchronize(h->stream), "set_field sync");
     return SF_OK;
+}
+
+sf_status sf_export_bgeo(sf_handle* h, int32_t scene, const char* folder_path, const char* file_name) {
+    if (!h) return SF_ERR_INVALID;
+    if (scene < 0 || scene >= h->nScenes || !file_name) return h->fail(SF_ERR_INVALID, "bad scene or file name");
+    const SceneDev& S = h->hScenes[scene];
+    const int64_t n = h->n[scene];
+    const size_t bytes = std::max<size_t>(16, size_t(n) * 36);
+    if (ensureStage(h, bytes) || ensurePinned(h->exportHost, h->exportHostBytes, bytes, h->err)) return SF_ERR_CUDA;
+    const int c = h->cur;
+    return exportBgeoSlots(h->stream, n, h->pos[c] + S.slot_off, h->col[c] + S.slot_off, h->mat[c] + S.slot_off,
+                           h->stage, h->exportHost, folder_path, file_name, h->err);
 }
 
 sf_status sf_get_cell_table(sf_handle* h, int32_t scene, int32_t which, int64_t* dst, int64_t count) {

@@ -12,7 +12,7 @@ using namespace KIRI;
 
 int main(int argc, char** argv) {
     if (argc < 3) {
-        std::fprintf(stderr, "usage: facade_main <dump> <frames>\n");
+        std::fprintf(stderr, "usage: facade_main <dump> <frames> [<bgeo export folder>]\n");
         return 2;
     }
     const int frames = std::atoi(argv[2]);
@@ -114,6 +114,13 @@ int main(int argc, char** argv) {
     std::fwrite(out.data(), sizeof(float), out.size(), f);
     std::fclose(f);
     float3* dpos = particles->GetPosPtr();
+    if (argc > 3) {  // the app's per-frame export (main.cpp:265-276) and a read-back
+        ExportBgeoFileCUDA(argv[3], UInt2Str4Digit(unsigned(frames)), particles->GetPosPtr(), particles->GetColPtr(),
+                           particles->GetRadiusPtr(), particles->GetLabelPtr(), particles->Size());
+        const Vec_Float4 back = ReadBgeoFileForGPU("out", UInt2Str4Digit(unsigned(frames)));
+        std::printf("bgeo read back: %zu points, first pscale %.6g\n", back.size(),
+                    back.empty() ? -1.0 : double(back[0].w));
+    }
     std::printf("facade ok: particles=%zu boundary=%zu frames=%d calls=%zu n_sub=%zu device_pos=%p\n", n,
                 boundary.pos.size(), frames, calls, system.GetNumOfSubTimeSteps(), static_cast<void*>(dpos));
     return dpos ? 0 : 6;

@@ -21,7 +21,8 @@ def build_program(tmp_path):
     cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
     exe = str(tmp_path / "facade_main")
     pkg = os.path.join(ROOT, "sph_seepage_flows_gb300")
-    cmd = ["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), "-I", f"{cuda}/include",
+    cmd = ["g++", "-std=c++17", "-O2", f'-DDB_PBR_PATH="{tmp_path}/"', "-I", os.path.join(ROOT, "include"),
+           "-I", f"{cuda}/include",
            os.path.join(ROOT, "tests", "cpp", "facade_main.cpp"), "-o", exe, "-L", pkg, "-l:libsf_gb300.so",
            f"-Wl,-rpath,{pkg}", "-L", f"{cuda}/lib64", "-lcudart"]
     subprocess.run(cmd, check=True)
@@ -46,7 +47,8 @@ def test_facade_program_matches_c_abi(cuda_lib, tmp_path):
     from sph_seepage_flows_gb300.capi import Simulation
     exe = build_program(tmp_path)
     dump = str(tmp_path / "dump.bin")
-    out = subprocess.run([exe, dump, "1"], capture_output=True, text=True, timeout=300)
+    export = tmp_path / "bgeo" / "out"   # the reader's DB_PBR_PATH "bgeo/out"
+    out = subprocess.run([exe, dump, "1", str(export)], capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stdout + out.stderr
     assert "facade ok" in out.stdout
     raw = np.fromfile(dump, dtype=np.float32)
@@ -57,3 +59,9 @@ def test_facade_program_matches_c_abi(cuda_lib, tmp_path):
     calls = sim.frame_adaptive(1.0 / 30.0)
     assert f"calls={calls}" in out.stdout
     np.testing.assert_array_equal(sim.field("pos", order="id"), final)
+    # ExportBgeoFileCUDA of the final frame: the oracle's bytes for the same
+    # arrays in the current (sorted) order, read back by ReadBgeoFileForGPU
+    from oracle import bgeo
+    data = (export / "0001.bgeo").read_bytes()
+    assert data == bgeo.write_bytes(sim.field("pos"), sim.field("col"), sim.field("radius"), sim.field("label"))
+    assert f"bgeo read back: {sc.n} points" in out.stdout
