@@ -32,6 +32,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <memory>
 #include <random>
 #include <string>
@@ -500,8 +501,10 @@ public:
                                           float sandDensity, float3 cda0asat, float2 amcamcp, bool offsetY,
                                           float worldLowestY) const {
         if (!bEnable) return;
-        if (data.pos.empty()) data.sandMinRadius = 3.4e38f;
-        float minY = 3.4e38f;
+        // Huge<size_t>() of the reference, as a float
+        const float huge = static_cast<float>(std::numeric_limits<size_t>::max());
+        if (data.pos.empty()) data.sandMinRadius = huge;
+        float minY = huge;
         for (const float4& s : shape) {
             data.pos.push_back(make_float3(s.x, s.y, s.z));
             data.col.push_back(color);

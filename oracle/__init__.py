@@ -251,6 +251,14 @@ def ref_lib():
         lib.sfref_emitter_points.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
                                              ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                              ctypes.POINTER(ctypes.c_float), ctypes.c_int64]
+        F = ctypes.POINTER(ctypes.c_float)
+        lib.sfref_shape_multi_volume.restype = ctypes.c_int64
+        lib.sfref_shape_multi_volume.argtypes = [F, ctypes.c_int64, F, ctypes.c_float, F, F, ctypes.c_int,
+                                                 ctypes.c_float, ctypes.c_int, F, F, F, F, F, F,
+                                                 ctypes.POINTER(ctypes.c_int32), ctypes.c_int64, F]
+        lib.sfref_boundary_shape_volume.restype = ctypes.c_int64
+        lib.sfref_boundary_shape_volume.argtypes = [F, ctypes.c_int64, F, ctypes.POINTER(ctypes.c_int32),
+                                                    ctypes.c_int64]
         _REF_LIB = lib
     return _REF_LIB
 
@@ -287,6 +295,39 @@ def ref_world_boundary(lowest, highest, particle_radius):
     out = np.zeros((n, 3), np.float32)
     lab = np.zeros(n, np.int32)
     lib.sfref_world_boundary(_fptr(lo), _fptr(hi), float(particle_radius), _fptr(out), _iptr(lab), min(n, cap))
+    return out, lab
+
+
+def ref_shape_multi_volume(shape, color, density, cda0asat, amcamcp, offset_y, lowest_y, twice=False):
+    """The reference's BuildSeepageflowShapeMultiVolume on shape (n, 4): a dict
+    of its output arrays and sand_min_radius."""
+    lib = ref_lib()
+    sh = np.ascontiguousarray(shape, np.float32)
+    n = len(sh) * (2 if twice else 1)
+    out = {"pos": np.zeros((n, 3), np.float32), "col": np.zeros((n, 3), np.float32),
+           "cda0asat": np.zeros((n, 3), np.float32), "radius": np.zeros(n, np.float32),
+           "mass": np.zeros(n, np.float32), "amcamcp": np.zeros((n, 2), np.float32),
+           "label": np.zeros(n, np.int32)}
+    smr = ctypes.c_float()
+    c = np.asarray(color, np.float32)
+    cda = np.asarray(cda0asat, np.float32)
+    amc = np.asarray(amcamcp, np.float32)
+    cnt = lib.sfref_shape_multi_volume(_fptr(sh), len(sh), _fptr(c), float(density), _fptr(cda), _fptr(amc),
+                                       int(offset_y), float(lowest_y), int(twice), _fptr(out["pos"]),
+                                       _fptr(out["col"]), _fptr(out["cda0asat"]), _fptr(out["radius"]),
+                                       _fptr(out["mass"]), _fptr(out["amcamcp"]), _iptr(out["label"]), n,
+                                       ctypes.byref(smr))
+    assert cnt == n
+    out["sand_min_radius"] = np.float32(smr.value)
+    return out
+
+
+def ref_boundary_shape_volume(shape):
+    lib = ref_lib()
+    sh = np.ascontiguousarray(shape, np.float32)
+    out = np.zeros((len(sh), 3), np.float32)
+    lab = np.zeros(len(sh), np.int32)
+    lib.sfref_boundary_shape_volume(_fptr(sh), len(sh), _fptr(out), _iptr(lab), len(sh))
     return out, lab
 
 

@@ -438,4 +438,59 @@ int64_t sfref_emitter_points(const float pos[3], const float vel[3], int type, f
     return cnt;
 }
 
+// CudaVolumeEmitter::BuildSeepageflowShapeMultiVolume (cuda_volume_emitter.cpp:
+// 137-175), the reference's own code, on n shape points (x, y, z, radius),
+// called twice when `twice` (two objects gathered into one volume, as the
+// app's loop over shape files does). Writes per particle pos, col, cda0asat
+// (3 floats), radius, mass (1), amcamcp (2), label; returns the count (at most
+// cap written) and the data's sandMinRadius.
+int64_t sfref_shape_multi_volume(const float* shape, int64_t n, const float color[3], float density,
+                                 const float cda0asat[3], const float amcamcp[2], int offset_y, float lowest_y,
+                                 int twice, float* out_pos, float* out_col, float* out_cda, float* out_radius,
+                                 float* out_mass, float* out_amc, int32_t* out_label, int64_t cap,
+                                 float* sand_min_radius) {
+    Vec_Float4 sh;
+    for (int64_t i = 0; i < n; ++i) sh.push_back(make_float4(shape[4 * i], shape[4 * i + 1], shape[4 * i + 2], shape[4 * i + 3]));
+    SeepageflowMultiVolumeData data;
+    CudaVolumeEmitter em;
+    for (int k = 0; k < (twice ? 2 : 1); ++k)
+        em.BuildSeepageflowShapeMultiVolume(data, sh, make_float3(color[0], color[1], color[2]), density,
+                                            make_float3(cda0asat[0], cda0asat[1], cda0asat[2]),
+                                            make_float2(amcamcp[0], amcamcp[1]), offset_y != 0, lowest_y);
+    const int64_t cnt = int64_t(data.pos.size());
+    for (int64_t i = 0; i < std::min(cnt, cap); ++i) {
+        const float3 v3[3] = {data.pos[i], data.col[i], data.cda0asat[i]};
+        float* o3[3] = {out_pos, out_col, out_cda};
+        for (int a = 0; a < 3; ++a) {
+            o3[a][3 * i] = v3[a].x;
+            o3[a][3 * i + 1] = v3[a].y;
+            o3[a][3 * i + 2] = v3[a].z;
+        }
+        out_radius[i] = data.radius[i];
+        out_mass[i] = data.mass[i];
+        out_amc[2 * i] = data.amcamcp[i].x;
+        out_amc[2 * i + 1] = data.amcamcp[i].y;
+        out_label[i] = int32_t(data.label[i]);
+    }
+    *sand_min_radius = data.sandMinRadius;
+    return cnt;
+}
+
+// CudaBoundaryEmitter::BuildBoundaryShapeVolume (cuda_boundary_emitter.cpp:82-92).
+int64_t sfref_boundary_shape_volume(const float* shape, int64_t n, float* out_pos, int32_t* out_label, int64_t cap) {
+    Vec_Float4 sh;
+    for (int64_t i = 0; i < n; ++i) sh.push_back(make_float4(shape[4 * i], shape[4 * i + 1], shape[4 * i + 2], shape[4 * i + 3]));
+    BoundaryData data;
+    CudaBoundaryEmitter em;
+    em.BuildBoundaryShapeVolume(data, sh);
+    const int64_t cnt = int64_t(data.pos.size());
+    for (int64_t i = 0; i < std::min(cnt, cap); ++i) {
+        out_pos[3 * i] = data.pos[i].x;
+        out_pos[3 * i + 1] = data.pos[i].y;
+        out_pos[3 * i + 2] = data.pos[i].z;
+        out_label[i] = int32_t(data.label[i]);
+    }
+    return cnt;
+}
+
 }  // extern "C"

@@ -190,6 +190,30 @@ def tiny(seed: int = 7, sand=(10, 8, 10), water=(8, 12, 10)) -> Scene:
                        water_origin=(0.4 - 0.02 - (sand[0] - 1 + water[0]) * pitch, 0.02, 0.06))
 
 
+def add_shape_boundary(scene: Scene, points) -> Scene:
+    """Appends shape boundary particles (label 1), as
+    CudaBoundaryEmitter::BuildBoundaryShapeVolume does with the points of a
+    shape file (cuda_boundary_emitter.cpp:82-92): sand collides with them
+    (DEM) and water is pushed out of them at the end of every substep."""
+    pts = np.asarray(points, np.float32).reshape(-1, 3)
+    scene.bpos = np.concatenate([scene.bpos, pts]).astype(np.float32)
+    scene.blabel = np.concatenate([scene.blabel, np.ones(len(pts), np.int32)])
+    return scene
+
+
+def tiny_with_plate(seed: int = 21) -> Scene:
+    """tiny() standing on a shape-boundary plate (label 1) at z = 0.055, 5 mm
+    below the lowest particle layer: the sand block rests on it through DEM
+    contacts and the water above it is pushed out of its 2r shell."""
+    sc = tiny(seed=seed)
+    xs = np.arange(0.03, 0.39, 0.01, dtype=np.float32)
+    ys = np.arange(0.01, 0.39, 0.01, dtype=np.float32)
+    gx, gy = np.meshgrid(xs, ys, indexing="ij")
+    plate = np.stack([gx.ravel(), gy.ravel(), np.full(gx.size, 0.055, np.float32)], axis=1)
+    sc.name = "tiny_plate"
+    return add_shape_boundary(sc, plate)
+
+
 def _axis(start, stop, pitch):
     """Lattice coordinates start + k*pitch <= stop (k = 0, 1, ...)."""
     if stop < start:

@@ -9,7 +9,10 @@ Fixtures (float32 / int32 arrays, cell-sorted order as the reference getters):
   tiny_multi_wcsph.npz  tiny scene, MULTI_SF + WCSPH: inputs, state after 1
                         and after 10 adaptive substeps (UpdateSystem(1/30))
   tiny_sf_sph.npz       same scene with SF + plain SPH: state after 1 substep
+  tiny_plate.npz        tiny scene on a shape-boundary plate (label 1 boundary
+                        particles): inputs, state after 1 substep
   emitters.npz          world-boundary shell and emitter sample points
+  shapes.npz            the shape-volume builders on a seeded stand-in shape
 """
 
 import os
@@ -85,9 +88,41 @@ def main():
     for kind, name, a, b in ((0, "square", 0.05, 0.0), (1, "circle", 0.17, 0.0), (2, "rectangle", 0.22, 0.18)):
         em["emit_" + name] = oracle.ref_emitter_points((0.9, 0.9, 1.25), (0.0, 0.0, -5.0), kind, 0.01, a, b)
     np.savez_compressed(os.path.join(OUT, "emitters.npz"), **em)
+    shape_goldens()
+    plate_golden()
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)), "bytes")
+
+
+def plate_golden():
+    """Shape boundary particles in a substep: tiny scene on a label-1 plate."""
+    sc = scenes.tiny_with_plate()
+    r = oracle.RefHarness(sc)
+    d = {**inputs(sc), **params_arrays(sc)}
+    r.substeps(1.0 / 30.0, True, 1)
+    d.update(snapshot(r, "s1"))
+    np.savez_compressed(os.path.join(OUT, "tiny_plate.npz"), **d)
+
+
+def shape_goldens():
+    """The reference's shape-volume builders (the app's bunny/dam import path)
+    on a seeded stand-in shape: 300 points in a ball with radii 4-6 mm."""
+    import oracle
+    rng = np.random.default_rng(2024)
+    d = rng.normal(size=(300, 3))
+    d *= (0.1 * rng.random(300) ** (1 / 3) / np.linalg.norm(d, axis=1))[:, None]
+    shape = np.empty((300, 4), np.float32)
+    shape[:, :3] = d + np.array([0.5, 0.3, 0.5])
+    shape[:, 3] = 0.004 + 0.002 * rng.random(300)
+    g = {"shape": shape}
+    args = dict(color=(0.88, 0.79, 0.62), density=2650.0, cda0asat=(0.5, 0.6, 0.8), amcamcp=(0.7, 0.3))
+    for tag, off, twice in (("plain", False, False), ("offset", True, False), ("offset_twice", True, True)):
+        out = oracle.ref_shape_multi_volume(shape, offset_y=off, lowest_y=0.02, twice=twice, **args)
+        for k, v in out.items():
+            g[f"{tag}_{k}"] = v
+    g["bshape_pos"], g["bshape_label"] = oracle.ref_boundary_shape_volume(shape)
+    np.savez_compressed(os.path.join(OUT, "shapes.npz"), **g)
 
 
 if __name__ == "__main__":

@@ -101,14 +101,16 @@ def dense_cluster_scene():
 
 
 @pytest.mark.parametrize("lanes", [0, 1])
-@pytest.mark.parametrize("which", ["tiny", "dense"])
+@pytest.mark.parametrize("which", ["tiny", "dense", "plate"])
 def test_stages_bit_exact_against_fp32_oracle(cuda_lib, oracle_mod, which, lanes):
     """Each stage on identical inputs: the GPU output equals the FP32 oracle's
     bit-for-bit for every field free of powf and of reordered sums, within TOL
-    otherwise. "dense" exercises the neighbour-list overflow fallback. lanes 0
+    otherwise. "dense" exercises the neighbour-list overflow fallback, "plate"
+    the shape boundary particles (label 1: sand DEM, water push-out). lanes 0
     is the automatic choice for these small scenes (8 threads per particle);
     lanes 1 is the one-thread-per-particle path that large scenes take."""
-    sc = scenes.tiny(seed=11) if which == "tiny" else dense_cluster_scene()
+    sc = {"tiny": lambda: scenes.tiny(seed=11), "dense": dense_cluster_scene,
+          "plate": scenes.tiny_with_plate}[which]()
     sim = gpu_sim(sc)
     sim.set_lanes(lanes)
     o32 = oracle_mod.Oracle(sc, 32)
@@ -166,6 +168,18 @@ def test_ten_substeps_track_reference(cuda_lib):
     assert np.abs(pos - ref).max() < 1e-6
     dens = sim.field("density")[order]
     assert rel_err(dens, g["s10_density"][ref_order]) < 1e-4
+
+
+def test_shape_plate_substep_tracks_reference(cuda_lib):
+    """One adaptive substep on the shape-boundary plate scene against the
+    reference kernels' fixture (tiny_plate.npz)."""
+    g = load_golden("tiny_plate.npz")
+    sim = gpu_sim(scene_from_golden(g))
+    sim.step(T_FRAME)
+    assert sim.num_substeps() == int(g["s1_n_sub"])
+    order, ref_order = np.argsort(sim.field("id")), np.argsort(g["s1_id"])
+    assert np.abs(sim.field("pos")[order] - g["s1_pos"][ref_order]).max() < 1e-6
+    assert np.array_equal(sim.cell_table(0), g["s1_cell_start"].astype(np.int64))
 
 
 def test_fixed_dt_graph_equals_eager(cuda_lib):

@@ -12,7 +12,7 @@ T = 1.0 / 30.0
 NAMES = [k for k in FIELDS if k not in ("key", "neighbors")]
 
 
-@pytest.mark.parametrize("fixture", ["tiny_multi_wcsph.npz", "tiny_sf_sph.npz"])
+@pytest.mark.parametrize("fixture", ["tiny_multi_wcsph.npz", "tiny_sf_sph.npz", "tiny_plate.npz"])
 def test_fp32_oracle_bit_exact_after_one_substep(oracle_mod, fixture):
     g = load_golden(fixture)
     o = oracle_mod.Oracle(scene_from_golden(g), 32)

@@ -46,6 +46,23 @@ def test_oracle_bit_exact_with_reference_kernels(harness, name, kw, override):
             assert np.array_equal(o.field(f), ref.field(f)), (step, f)
 
 
+def test_shape_boundary_plate(harness):
+    """Shape boundary particles (label 1): sand DEM against them and the
+    water push-out of the integrator."""
+    sc = scenes.tiny_with_plate()
+    assert (sc.blabel == 1).sum() > 1000
+    ref = harness.RefHarness(sc)
+    o = harness.Oracle(sc, 32)
+    for step in range(4):
+        ref.substeps(T, True, 1)
+        o.substeps(T, True, 1)
+        assert o.num_substeps == ref.num_substeps
+        for f in FIELDS:
+            if f in ("key", "neighbors"):
+                continue
+            assert np.array_equal(o.field(f), ref.field(f)), (step, f)
+
+
 def test_moving_water_column_with_velocities(harness):
     sc = scenes.tiny(seed=35)
     rng = np.random.default_rng(0)
