@@ -301,7 +301,9 @@ void launchCellStart(cudaStream_t s, int n, int nCells, const unsigned int* sort
 
 // cellStart[c] = v for c in [lo, hi), written by the lanes of one warp
 // (all 32 call it): short runs by their own lane, long runs (the empty cells
-// before a sparse region) by the whole warp, one run after the other.
+// before a sparse region, up to whole empty slabs of the grid) by the whole
+// warp, one run after the other, in 16-byte stores (the table is 16-byte
+// aligned).
 __device__ __forceinline__ void fillCellRuns(unsigned int* __restrict__ cs, unsigned int lo, unsigned int hi,
                                              unsigned int v) {
     constexpr unsigned int kShort = 8;
@@ -312,7 +314,11 @@ __device__ __forceinline__ void fillCellRuns(unsigned int* __restrict__ cs, unsi
         const int src = __ffs(longRuns) - 1;
         const unsigned int l = __shfl_sync(0xffffffffu, lo, src), h = __shfl_sync(0xffffffffu, hi, src);
         const unsigned int w = __shfl_sync(0xffffffffu, v, src);
-        for (unsigned int c = l + lane; c < h; c += 32u) cs[c] = w;
+        const unsigned int a = min(h, (l + 3u) & ~3u), b = a + ((h - a) & ~3u);  // [a, b): whole 16-byte words
+        if (lane < a - l) cs[l + lane] = w;
+        if (lane < h - b) cs[b + lane] = w;
+        const uint4 w4 = make_uint4(w, w, w, w);
+        for (unsigned int q = a / 4u + lane; q < b / 4u; q += 32u) reinterpret_cast<uint4*>(cs)[q] = w4;
     }
 }
 
