@@ -60,8 +60,8 @@ BYTES_PER_SUBSTEP = sum(STAGE_BYTES.values())  # 753
 
 # DRAM bytes (read + write) per launch of each stage's main kernel on the 1M
 # workload, from the committed ncu capture (profiles/neighbor_passes_1M_ncu.md).
-NCU_TRAFFIC = {"density": 289.0e6, "avgflow": 120.5e6, "water_momentum": 135.1e6,
-               "sand_momentum": 55.6e6, "voidage_adhesion": 60.5e6}
+NCU_TRAFFIC = {"density": 283.9e6, "avgflow": 137.1e6, "water_momentum": 139.3e6,
+               "sand_momentum": 65.8e6, "voidage_adhesion": 65.0e6}
 
 
 def peaks():
