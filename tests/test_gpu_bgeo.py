@@ -61,3 +61,22 @@ def test_large_scene_export_parses_to_its_fields(cuda_lib, tmp_path):
     assert np.array_equal(a["position"], pos) and np.array_equal(a["Cd"], col)
     assert np.array_equal(a["pscale"][:, 0], rad) and np.array_equal(a["label"][:, 0], lab)
     sim.close()
+
+
+def test_batched_handle_exports_each_scene(cuda_lib, tmp_path):
+    """Each scene of a batched handle exports its own particles (its slot
+    range of the scene-offset layout), equal to a single-scene handle's file."""
+    from sph_seepage_flows_gb300.capi import Simulation
+    scs = [scenes.tiny(seed=s) for s in (7, 8, 9)]
+    scs[1] = scenes.tiny(seed=8, sand=(6, 6, 6), water=(5, 7, 6))   # a different size
+    dt = reference_dt(scs[0].params, scs[0].bparams, scs[0].sparams)[1]
+    sim = Simulation(scs)
+    sim.substeps_fixed(dt, 3)
+    for k, sc in enumerate(scs):
+        sim.export_bgeo(str(tmp_path), f"scene{k}", scene=k)
+        one = Simulation(sc)
+        one.substeps_fixed(dt, 3)
+        one.export_bgeo(str(tmp_path), f"single{k}")
+        assert (tmp_path / f"scene{k}.bgeo").read_bytes() == (tmp_path / f"single{k}.bgeo").read_bytes(), k
+        one.close()
+    sim.close()

@@ -154,6 +154,39 @@ def test_stages_bit_exact_against_fp32_oracle(cuda_lib, oracle_mod, which, lanes
                 o32.set_field(name, sim.field(name))
 
 
+def test_fields_set_between_stages_reach_the_momentum_passes(cuda_lib, oracle_mod):
+    """sf_set_field between the voidage/adhesion pass and the momentum passes:
+    the values the passes derived from the changed fields (the water (D, P)
+    pairs, the gather records, the adhesion Bezier factor) are recomputed, so
+    the momentum passes see the new fields as the reference's kernels would."""
+    sc = scenes.tiny(seed=13)
+    sim = gpu_sim(sc)
+    o32 = oracle_mod.Oracle(sc, 32)
+    for st in ("sort", "density", "avgflow", "voidage_adhesion"):
+        sim.stage(st, T_FRAME, adaptive=True)
+        o32.stage(st, T_FRAME, adaptive=True)
+    for name in ("pos", "vel", "density", "pressure", "voidage", "saturation", "avg_flow", "adhesion",
+                 "avg_adhesion", "col", "max_saturation"):
+        o32.set_field(name, sim.field(name))
+    rng = np.random.default_rng(5)
+    n = sc.n
+    sand = sim.field("label") == 1
+    vel = (sim.field("vel") + rng.normal(0, 0.05, (n, 3))).astype(np.float32)
+    sat = np.where(sand, rng.random(n), sim.field("saturation")).astype(np.float32)
+    prs = (sim.field("pressure") * rng.uniform(0.9, 1.1, n)).astype(np.float32)
+    void = np.where(sand, rng.uniform(0.35, 0.65, n), rng.uniform(0.5, 1.0, n)).astype(np.float32)
+    dens = (sim.field("density") * np.where(sand, 1.0, rng.uniform(0.98, 1.02, n))).astype(np.float32)
+    for name, v in (("vel", vel), ("saturation", sat), ("pressure", prs), ("voidage", void), ("density", dens)):
+        sim.set_field(name, v)
+        o32.set_field(name, v)
+    for st, lab in (("sand_momentum", 1), ("water_momentum", 0)):
+        sim.stage(st, T_FRAME, adaptive=True)
+        o32.stage(st, T_FRAME, adaptive=True)
+        keep = sim.field("label") == lab
+        err = rel_err(sim.field("acc")[keep], o32.field("acc")[keep], o32.field("acc_scale")[keep])
+        assert err <= TOL, (st, err)
+
+
 def test_ten_substeps_track_reference(cuda_lib):
     g = load_golden("tiny_multi_wcsph.npz")
     sim = gpu_sim(scene_from_golden(g))
