@@ -293,6 +293,12 @@ public:
     float3 GetHighestPoint() const { return mHighestPoint; }
     float GetCellSize() const { return mCellSize; }
     int3 GetGridSize() const { return mGridSize; }
+    // CudaGNBaseSearcher::GetCellStartPtr (cuda_neighbor_searcher.cuh:35-44):
+    // device array of G + 1 size_t, the start of every cell in the sorted
+    // particles (boundary particles for the boundary searcher) and the count
+    // at entry G. A copy of the table of the last sort, refreshed by each
+    // call; nullptr before the searcher's system exists.
+    size_t* GetCellStartPtr() const;
 
 protected:
     static float3 f3div(float3 a, float s) { return make_float3(a.x / s, a.y / s, a.z / s); }
@@ -300,6 +306,10 @@ protected:
     float mCellSize;
     size_t mMaxNumOfParticles;
     int3 mGridSize;
+    CudaSFSystem* mSystem = nullptr;
+    int mTable = 0;  // 0: particle cell table, 1: boundary cell table
+    mutable detail::DeviceBuffer mCellBuf;
+    friend class CudaSFSystem;
 };
 
 class CudaGNSearcher final : public CudaGNBaseSearcher {
@@ -317,7 +327,9 @@ using CudaGNSearcherPtr = SharedPtr<CudaGNSearcher>;
 class CudaGNBoundarySearcher final : public CudaGNBaseSearcher {
 public:
     CudaGNBoundarySearcher(const float3 lp, const float3 hp, const size_t num, const float cellSize)
-        : CudaGNBaseSearcher(lp, hp, num, cellSize) {}
+        : CudaGNBaseSearcher(lp, hp, num, cellSize) {
+        mTable = 1;
+    }
 };
 using CudaGNBoundarySearcherPtr = SharedPtr<CudaGNBoundarySearcher>;
 
@@ -602,6 +614,8 @@ public:
         }
         mParticles->mSystem = this;
         mBoundaries->mSystem = this;
+        if (mSearcher) mSearcher->mSystem = this;
+        if (mBoundarySearcher) mBoundarySearcher->mSystem = this;
     }
     ~CudaSFSystem() {
         if (mHandle) sf_destroy(mHandle);
@@ -683,6 +697,20 @@ inline size_t CudaParticles::Size() const {
     int64_t n = 0, cap = 0;
     sf_size(mSystem->Handle(), 0, &n, &cap);
     return size_t(n);
+}
+
+inline size_t* CudaGNBaseSearcher::GetCellStartPtr() const {
+    if (!mSystem || !mSystem->Handle()) return nullptr;
+    int32_t g[3];
+    int64_t cells = 0;
+    if (sf_get_grid(mSystem->Handle(), 0, g, &cells) != SF_OK) return nullptr;
+    std::vector<int64_t> t(size_t(cells) + 1);
+    if (sf_get_cell_table(mSystem->Handle(), 0, mTable, t.data(), int64_t(t.size())) != SF_OK) return nullptr;
+    std::vector<size_t> ts(t.begin(), t.end());
+    void* d = mCellBuf.reserve(ts.size() * sizeof(size_t));
+    if (!d || cudaMemcpy(d, ts.data(), ts.size() * sizeof(size_t), cudaMemcpyHostToDevice) != cudaSuccess)
+        return nullptr;
+    return static_cast<size_t*>(d);
 }
 
 inline void* CudaSFParticles::field(int id, size_t elemBytes) const {

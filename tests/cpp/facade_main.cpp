@@ -114,6 +114,19 @@ int main(int argc, char** argv) {
     std::fwrite(out.data(), sizeof(float), out.size(), f);
     std::fclose(f);
     float3* dpos = particles->GetPosPtr();
+    // the searchers' cell tables (GetCellStartPtr): G + 1 monotone entries
+    // ending with the particle / boundary count
+    for (int which = 0; which < 2; ++which) {
+        const CudaGNBaseSearcher& se = which ? static_cast<const CudaGNBaseSearcher&>(*boundarySearcher)
+                                             : static_cast<const CudaGNBaseSearcher&>(*searcher);
+        const int3 g = se.GetGridSize();
+        std::vector<size_t> t(size_t(g.x) * g.y * g.z + 1);
+        size_t* d = se.GetCellStartPtr();
+        if (!d || cudaMemcpy(t.data(), d, t.size() * sizeof(size_t), cudaMemcpyDeviceToHost) != cudaSuccess) return 7;
+        bool mono = true;
+        for (size_t c = 1; c < t.size(); ++c) mono = mono && t[c] >= t[c - 1];
+        std::printf("cell table %d: entries=%zu last=%zu monotone=%d\n", which, t.size(), t.back(), int(mono));
+    }
     if (argc > 3) {  // the app's per-frame export (main.cpp:265-276) and a read-back
         ExportBgeoFileCUDA(argv[3], UInt2Str4Digit(unsigned(frames)), particles->GetPosPtr(), particles->GetColPtr(),
                            particles->GetRadiusPtr(), particles->GetLabelPtr(), particles->Size());

@@ -65,3 +65,7 @@ def test_facade_program_matches_c_abi(cuda_lib, tmp_path):
     data = (export / "0001.bgeo").read_bytes()
     assert data == bgeo.write_bytes(sim.field("pos"), sim.field("col"), sim.field("radius"), sim.field("label"))
     assert f"bgeo read back: {sc.n} points" in out.stdout
+    # the searchers' GetCellStartPtr tables equal the C ABI's
+    nc = sim.cell_table(0).size
+    assert f"cell table 0: entries={nc} last={sc.n} monotone=1" in out.stdout
+    assert f"cell table 1: entries={nc} last={sc.nb} monotone=1" in out.stdout
