@@ -713,10 +713,8 @@ __global__ void __launch_bounds__(kSlotAlign) kAdjSandPairs(const SceneDev* __re
 
 // A4a: sand: voidage = num / den -> (num-bar, den-bar); water: adhesion
 // cotangent total (F_adh-bar + avg-bar / v_s) and v_s-bar.
-__global__ void __launch_bounds__(kSlotAlign) kAdjVoidSelf(const SceneDev* __restrict__ scenes,
-                                                           const int* __restrict__ blockScene, AdjBuffers A,
-                                                           PassBuffers b) {
-    SF_ADJ_PROLOGUE
+__global__ void __launch_bounds__(kSlotAlign) kAdjVoidSelf(AdjBuffers A, PassBuffers b) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     const float4 pk4 = b.pos4[slot];
     if (pk4.w == 0.f) return;
     const float3 xk = xyz(pk4);
@@ -997,7 +995,7 @@ int launchAdjSubstep(const LaunchCtx& c, const AdjBuffers& A, const PassBuffers&
     launchPairs(c, A, b, paramPartial, lanes, 0);
     kAdjSandSelf<<<g, t, 0, s>>>(c.scenes, c.blockScene, A, b, paramPartial, lanes);
     launchPairs(c, A, b, paramPartial, lanes, 1);
-    kAdjVoidSelf<<<g, t, 0, s>>>(c.scenes, c.blockScene, A, b);
+    kAdjVoidSelf<<<g, t, 0, s>>>(A, b);
     launchPairs(c, A, b, paramPartial, lanes, 2);
     kAdjFlowSelf<<<g, t, 0, s>>>(A, b);
     launchPairs(c, A, b, paramPartial, lanes, 3);

@@ -121,29 +121,33 @@ void launchKeysHist(const LaunchCtx& c, int n, const float4* pos4, unsigned int*
     }
 }
 
-// Per-digit exclusive scan over tiles: block d scans hist[d * tiles ..
-// d * tiles + tiles) in place and writes the digit's total.
-__global__ void __launch_bounds__(kSortThreads) kScanTiles(unsigned int* __restrict__ hist, int tiles,
-                                                           unsigned int* __restrict__ digitTotal) {
-    __shared__ unsigned int part[kSortThreads];
-    unsigned int* h = hist + size_t(blockIdx.x) * tiles;
+// Per-digit exclusive scan over tiles, one warp per digit: warp d scans
+// hist[d * tiles .. d * tiles + tiles) in place, 32 tiles per step with
+// shuffles (the next 32 counts are loaded before the current ones are
+// scanned), and writes the digit's total.
+constexpr int kScanWarps = 8;
+__global__ void __launch_bounds__(kScanWarps * 32) kScanTiles(unsigned int* __restrict__ hist, int tiles,
+                                                              unsigned int* __restrict__ digitTotal, int digits) {
+    const int d = blockIdx.x * kScanWarps + int(threadIdx.x >> 5);
+    if (d >= digits) return;  // whole warps
+    const int lane = int(threadIdx.x & 31u);
+    unsigned int* h = hist + size_t(d) * tiles;
     unsigned int carry = 0;
-    for (int base = 0; base < tiles; base += kSortThreads) {
-        const int t = base + threadIdx.x;
-        const unsigned int v = t < tiles ? h[t] : 0u;
-        part[threadIdx.x] = v;
-        __syncthreads();
-        for (int o = 1; o < kSortThreads; o <<= 1) {
-            const unsigned int u = threadIdx.x >= o ? part[threadIdx.x - o] : 0u;
-            __syncthreads();
-            part[threadIdx.x] += u;
-            __syncthreads();
+    unsigned int next = lane < tiles ? h[lane] : 0u;
+    for (int base = 0; base < tiles; base += 32) {
+        const unsigned int v = next;
+        const int t = base + lane;
+        next = t + 32 < tiles ? h[t + 32] : 0u;
+        unsigned int incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned int u = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += u;
         }
-        if (t < tiles) h[t] = carry + part[threadIdx.x] - v;
-        carry += part[kSortThreads - 1];
-        __syncthreads();
+        if (t < tiles) h[t] = carry + incl - v;
+        carry += __shfl_sync(0xffffffffu, incl, 31);
     }
-    if (threadIdx.x == 0) digitTotal[blockIdx.x] = carry;
+    if (lane == 0) digitTotal[d] = carry;
 }
 
 template <int kSortItems, int kBits>
@@ -227,7 +231,8 @@ static void launchPassT(cudaStream_t s, int n, int shift, const unsigned int* kI
                         unsigned int* kOut, unsigned int* vOut, const SortScratch& sc, bool histDone) {
     const int tiles = sc.tiles;
     if (!histDone) kHist<kSortItems, kBits><<<tiles, kSortThreads, 0, s>>>(kIn, n, shift, sc.hist, tiles);
-    kScanTiles<<<1 << kBits, kSortThreads, 0, s>>>(sc.hist, tiles, sc.digitTotal);
+    kScanTiles<<<((1 << kBits) + kScanWarps - 1) / kScanWarps, kScanWarps * 32, 0, s>>>(sc.hist, tiles, sc.digitTotal,
+                                                                                       1 << kBits);
     kScatter<kSortItems, kBits><<<tiles, kSortThreads, 0, s>>>(kIn, vIn, kOut, vOut, n, shift, sc.hist, tiles,
                                                                sc.digitTotal);
 }
