@@ -43,11 +43,16 @@ __global__ void __launch_bounds__(kSortThreads) kHist(const unsigned int* __rest
     for (int q = 0; q < kPer; ++q) h[threadIdx.x * kPer + q] = 0;
     __syncthreads();
     const int base = blockIdx.x * kTile;
-#pragma unroll 4
+    // all of the thread's keys are loaded before the first shared-memory add
+    unsigned int k[kSortItems];
+#pragma unroll
     for (int r = 0; r < kSortItems; ++r) {
         const int idx = base + r * kSortThreads + threadIdx.x;
-        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & unsigned(R - 1)], 1u);
+        k[r] = idx < n ? keys[idx] : 0u;
     }
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r)
+        if (base + r * kSortThreads + int(threadIdx.x) < n) atomicAdd(&h[(k[r] >> shift) & unsigned(R - 1)], 1u);
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < kPer; ++q) {
@@ -72,11 +77,20 @@ __global__ void __launch_bounds__(kSortThreads) kKeysHist(const SceneDev* __rest
     for (int q = 0; q < kPer; ++q) h[threadIdx.x * kPer + q] = 0;
     __syncthreads();
     const int base = blockIdx.x * kTile;
-#pragma unroll 4
+    // all of the thread's positions are loaded before the first key
+    float4 p[kSortItems];
+    int sid[kSortItems];
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        const int slot = base + r * kSortThreads + threadIdx.x;
+        sid[r] = slot < n ? blockScene[slot / kSlotAlign] : 0;
+        p[r] = slot < n ? pos4[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
     for (int r = 0; r < kSortItems; ++r) {
         const int slot = base + r * kSortThreads + threadIdx.x;
         if (slot < n) {
-            const unsigned int k = slotKey(scenes[blockScene[slot / kSlotAlign]], pos4[slot], errWord);
+            const unsigned int k = slotKey(scenes[sid[r]], p[r], errWord);
             keys[slot] = k;
             atomicAdd(&h[k & unsigned(R - 1)], 1u);
         }
