@@ -209,15 +209,21 @@ __global__ void __launch_bounds__(kSortThreads) kScatter(const unsigned int* __r
     __syncthreads();
     const unsigned int ltMask = (1u << lane) - 1u;
     const int tileBase = blockIdx.x * kTile;
+    // the thread's keys and values of every round are loaded up front, so the
+    // rounds (three barriers each) do not wait for global loads
+    unsigned int kr[kSortItems], vr[kSortItems];
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        const int idx = tileBase + r * kSortThreads + tid;
+        kr[r] = idx < n ? keysIn[idx] : 0u;
+        vr[r] = idx < n ? (valsIn ? valsIn[idx] : unsigned(idx)) : 0u;
+    }
+#pragma unroll
     for (int r = 0; r < kSortItems; ++r) {
         const int idx = tileBase + r * kSortThreads + tid;
         const bool valid = idx < n;
-        unsigned int k = 0, v = 0, d = unsigned(R);
-        if (valid) {
-            k = keysIn[idx];
-            v = valsIn ? valsIn[idx] : unsigned(idx);
-            d = (k >> shift) & unsigned(R - 1);
-        }
+        const unsigned int k = kr[r], v = vr[r];
+        const unsigned int d = valid ? (k >> shift) & unsigned(R - 1) : unsigned(R);
         const unsigned int peers = __match_any_sync(0xffffffffu, d);
         const unsigned int rank = __popc(peers & ltMask);
         const bool leader = valid && rank == 0;
