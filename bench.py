@@ -398,12 +398,12 @@ def run_ours(args, rank, world):
         sim.field("vel", out=hv)
         e2e_steps = max(2, min(args.steps, 20))
 
+        inputs = {"pos": hp, "vel": hv}
+
         def e2e_step():
-            sim.set_field("pos", hp)
-            sim.set_field("vel", hv)
+            sim.set_fields(inputs)
             sim.substeps_fixed(dt, 1)
-            sim.field("pos", out=hp)
-            sim.field("vel", out=hv)
+            sim.get_fields(inputs)
 
         e2e_step()
         torch.cuda.synchronize()
@@ -419,7 +419,7 @@ def run_ours(args, rank, world):
             el = float(t.item())
         e2e = {"value": world * n * e2e_steps / el, "unit": "particle-substeps/s",
                "h2d_bytes_per_step": 2 * 12 * n, "d2h_bytes_per_step": 2 * 12 * n,
-               "path": "sf_set_field(pos, vel; pinned host) + sf_substeps_fixed(1) + sf_get_field(pos, vel)"}
+               "path": "sf_set_fields(pos, vel; pinned host) + sf_substeps_fixed(1) + sf_get_fields(pos, vel)"}
 
     flags = sim.check_error()
     # pair interactions per substep: for every particle, the particles within

@@ -19,6 +19,7 @@
  *   sf_num_substeps      CudaBaseSystem::GetNumOfSubTimeSteps (include/kiri_pbs_cuda/system/cuda_base_system.cuh:36)
  *   sf_frame_adaptive    the adaptive frame loop of seepage_flows/src/seepageflow/main.cpp:235-247
  *   sf_get_field         CudaSFParticles::Get*Ptr getters (include/kiri_pbs_cuda/particle/cuda_sf_particles.cuh:170-190)
+ *   sf_get_fields / sf_set_fields  several of those fields in one call (no reference counterpart)
  *   sf_get_cell_table    CudaGNBaseSearcher::GetCellStart / GetGridSize (include/kiri_pbs_cuda/searcher/cuda_neighbor_searcher.cuh:35-44)
  *   sf_export_bgeo       ExportBgeoFileCUDA (seepage_flows/include/kiri_utils.h:364-448) with a handle's particle arrays
  *   sf_export_bgeo_device ExportBgeoFileCUDA itself (device arrays in the reference's layout)
@@ -233,6 +234,15 @@ sf_status sf_get_field(sf_handle* h, int32_t scene, int32_t field, int32_t order
                        void* dst, int64_t count, int32_t dst_on_device);
 sf_status sf_set_field(sf_handle* h, int32_t scene, int32_t field, int32_t order,
                        const void* src, int64_t count, int32_t src_on_device);
+
+/* Several fields of one scene in one call: the copies of fields[k] to / from
+ * dsts[k] / srcs[k] are queued back to back and the call waits once (for host
+ * buffers), instead of once per field. Same rules per field as sf_get_field /
+ * sf_set_field. */
+sf_status sf_get_fields(sf_handle* h, int32_t scene, int32_t n_fields, const int32_t* fields, int32_t order,
+                        void* const* dsts, int64_t count, int32_t dst_on_device);
+sf_status sf_set_fields(sf_handle* h, int32_t scene, int32_t n_fields, const int32_t* fields, int32_t order,
+                        const void* const* srcs, int64_t count, int32_t src_on_device);
 
 /* Cell start table of one scene (which = 0 particles, 1 boundary), as
  * scene-relative offsets: G+1 entries, entry G = the scene's count. */

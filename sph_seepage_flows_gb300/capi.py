@@ -70,6 +70,8 @@ def load(path: str = LIB_PATH):
         "sf_run_stage": (i32, [H, i32, f32, i32]),
         "sf_get_field": (i32, [H, i32, i32, i32, ctypes.c_void_p, i64, i32]),
         "sf_set_field": (i32, [H, i32, i32, i32, ctypes.c_void_p, i64, i32]),
+        "sf_get_fields": (i32, [H, i32, i32, P(i32), i32, P(ctypes.c_void_p), i64, i32]),
+        "sf_set_fields": (i32, [H, i32, i32, P(i32), i32, P(ctypes.c_void_p), i64, i32]),
         "sf_get_cell_table": (i32, [H, i32, i32, P(i64), i64]),
         "sf_get_grid": (i32, [H, i32, P(i32), P(i64)]),
         "sf_size": (i32, [H, i32, P(i64), P(i64)]),
@@ -279,6 +281,22 @@ class Simulation:
         a = np.ascontiguousarray(values, dtype=dt)
         self._check(self.lib.sf_set_field(self.h, scene, fid, ORDER[order], a.ctypes.data_as(ctypes.c_void_p),
                                           self.size(scene), 0))
+
+    def get_fields(self, outs: dict, order: str = "sorted", scene: int = 0):
+        """sf_get_fields: {name: preallocated host array} filled in one call (one wait)."""
+        names = list(outs)
+        ids = (ctypes.c_int32 * len(names))(*[FIELDS[k][0] for k in names])
+        ptrs = (ctypes.c_void_p * len(names))(*[outs[k].ctypes.data for k in names])
+        self._check(self.lib.sf_get_fields(self.h, scene, len(names), ids, ORDER[order], ptrs, self.size(scene), 0))
+        return outs
+
+    def set_fields(self, values: dict, order: str = "sorted", scene: int = 0):
+        """sf_set_fields: {name: host array} written in one call (one wait)."""
+        arrs = {k: np.ascontiguousarray(v, dtype=FIELDS[k][2]) for k, v in values.items()}
+        names = list(arrs)
+        ids = (ctypes.c_int32 * len(names))(*[FIELDS[k][0] for k in names])
+        ptrs = (ctypes.c_void_p * len(names))(*[arrs[k].ctypes.data for k in names])
+        self._check(self.lib.sf_set_fields(self.h, scene, len(names), ids, ORDER[order], ptrs, self.size(scene), 0))
 
     def fields(self, names=None, order: str = "sorted", scene: int = 0) -> dict:
         return {k: self.field(k, order, scene) for k in (names or list(FIELDS.keys()))}

@@ -1203,8 +1203,12 @@ __global__ void kGetBoundary(int field, int n, int bOff, const float4* __restric
 
 }  // namespace
 
-sf_status sf_get_field(sf_handle* h, int32_t scene, int32_t field, int32_t order, void* dst, int64_t count,
-                       int32_t dst_on_device) {
+namespace {
+
+// sf_get_field without its final host synchronisation (the copy is queued on
+// the handle's stream).
+sf_status getFieldQueued(sf_handle* h, int32_t scene, int32_t field, int32_t order, void* dst, int64_t count,
+                         int32_t dst_on_device) {
     if (!h || !dst || scene < 0 || scene >= h->nScenes) return SF_ERR_INVALID;
     const int w = fieldWidth(field);
     if (w == 0) return h->fail(SF_ERR_INVALID, "unknown field");
@@ -1242,17 +1246,35 @@ sf_status sf_get_field(sf_handle* h, int32_t scene, int32_t field, int32_t order
                                                  h->sorted ? h->nbrCnt : nullptr, target);
     }
     if (h->cuda(cudaGetLastError(), "get_field launch")) return SF_ERR_CUDA;
-    if (!dst_on_device) {
-        if (!mapped &&
-            h->cuda(cudaMemcpyAsync(dst, h->stage, bytes, cudaMemcpyDeviceToHost, h->stream), "get_field D2H"))
-            return SF_ERR_CUDA;
-        return h->cuda(cudaStreamSynchronize(h->stream), "get_field sync");
-    }
+    if (!dst_on_device && !mapped &&
+        h->cuda(cudaMemcpyAsync(dst, h->stage, bytes, cudaMemcpyDeviceToHost, h->stream), "get_field D2H"))
+        return SF_ERR_CUDA;
     return SF_OK;
 }
 
-sf_status sf_set_field(sf_handle* h, int32_t scene, int32_t field, int32_t order, const void* src, int64_t count,
-                       int32_t src_on_device) {
+}  // namespace
+
+sf_status sf_get_field(sf_handle* h, int32_t scene, int32_t field, int32_t order, void* dst, int64_t count,
+                       int32_t dst_on_device) {
+    sf_status st = getFieldQueued(h, scene, field, order, dst, count, dst_on_device);
+    if (st || dst_on_device) return st;
+    return h->cuda(cudaStreamSynchronize(h->stream), "get_field sync");
+}
+
+sf_status sf_get_fields(sf_handle* h, int32_t scene, int32_t n_fields, const int32_t* fields, int32_t order,
+                        void* const* dsts, int64_t count, int32_t dst_on_device) {
+    if (!h || n_fields < 0 || (n_fields > 0 && (!fields || !dsts))) return SF_ERR_INVALID;
+    for (int32_t k = 0; k < n_fields; ++k)
+        if (sf_status st = getFieldQueued(h, scene, fields[k], order, dsts[k], count, dst_on_device)) return st;
+    if (dst_on_device || n_fields == 0) return SF_OK;
+    return h->cuda(cudaStreamSynchronize(h->stream), "get_fields sync");
+}
+
+namespace {
+
+// sf_set_field without its final host synchronisation.
+sf_status setFieldQueued(sf_handle* h, int32_t scene, int32_t field, int32_t order, const void* src, int64_t count,
+                         int32_t src_on_device) {
     if (!h || !src || scene < 0 || scene >= h->nScenes) return SF_ERR_INVALID;
     const int w = fieldWidth(field);
     if (w == 0 || field >= SF_BFIELD_POS || field == SF_FIELD_ID || field == SF_FIELD_KEY ||
@@ -1287,9 +1309,25 @@ sf_status sf_set_field(sf_handle* h, int32_t scene, int32_t field, int32_t order
                                                                h->vel[c], h->col[c], h->mat[c], h->amc[c], h->pid[c],
                                                                h->aux, h->flow, h->adh, h->avgadh, h->drag, h->acc,
                                                                h->dp, h->vrec2, h->grec4, from, h->dScenes + scene);
-    if (h->cuda(cudaGetLastError(), "set_field launch")) return SF_ERR_CUDA;
-    if (!src_on_device) return h->cuda(cudaStreamSynchronize(h->stream), "set_field sync");
-    return SF_OK;
+    return h->cuda(cudaGetLastError(), "set_field launch");
+}
+
+}  // namespace
+
+sf_status sf_set_field(sf_handle* h, int32_t scene, int32_t field, int32_t order, const void* src, int64_t count,
+                       int32_t src_on_device) {
+    sf_status st = setFieldQueued(h, scene, field, order, src, count, src_on_device);
+    if (st || src_on_device) return st;
+    return h->cuda(cudaStreamSynchronize(h->stream), "set_field sync");
+}
+
+sf_status sf_set_fields(sf_handle* h, int32_t scene, int32_t n_fields, const int32_t* fields, int32_t order,
+                        const void* const* srcs, int64_t count, int32_t src_on_device) {
+    if (!h || n_fields < 0 || (n_fields > 0 && (!fields || !srcs))) return SF_ERR_INVALID;
+    for (int32_t k = 0; k < n_fields; ++k)
+        if (sf_status st = setFieldQueued(h, scene, fields[k], order, srcs[k], count, src_on_device)) return st;
+    if (src_on_device || n_fields == 0) return SF_OK;
+    return h->cuda(cudaStreamSynchronize(h->stream), "set_fields sync");
 }
 
 sf_status sf_export_bgeo(sf_handle* h, int32_t scene, const char* folder_path, const char* file_name) {

@@ -303,3 +303,32 @@ def test_pinned_host_fields_match_staged(cuda_lib):
     pinned[:] = sim.field("vel") * np.float32(0.5)
     sim.set_field("vel", pinned)
     assert np.array_equal(sim.field("vel"), pinned)
+
+
+def test_multi_field_calls_equal_single_field_calls(cuda_lib):
+    """sf_set_fields / sf_get_fields (one wait for several fields), with pinned
+    and pageable host buffers, in both orders, equal the one-field calls."""
+    torch = pytest.importorskip("torch")
+    sc = scenes.tiny(seed=5)
+    a, b = gpu_sim(sc), gpu_sim(sc)
+    for s in (a, b):
+        s.substeps_fixed(2.0e-4, 3)
+    rng = np.random.default_rng(2)
+    for order in ("sorted", "id"):
+        new = {"pos": (a.field("pos", order) + rng.normal(0, 1e-4, (sc.n, 3))).astype(np.float32),
+               "vel": rng.normal(0, 0.1, (sc.n, 3)).astype(np.float32),
+               "saturation": rng.random(sc.n).astype(np.float32)}
+        for k, v in new.items():
+            a.set_field(k, v, order)
+        pinned = {}
+        for k, v in new.items():
+            pinned[k] = torch.empty(v.shape, dtype=torch.float32, pin_memory=True).numpy()
+            pinned[k][:] = v
+        b.set_fields(pinned if order == "sorted" else new, order)
+        outs = {k: torch.empty(v.shape, dtype=torch.float32, pin_memory=True).numpy() for k, v in new.items()}
+        b.get_fields(outs, order)
+        for k in new:
+            assert np.array_equal(outs[k], a.field(k, order)), (order, k)
+        a.substeps_fixed(2.0e-4, 2)
+        b.substeps_fixed(2.0e-4, 2)
+        assert np.array_equal(a.field("pos", "id"), b.field("pos", "id")), order
