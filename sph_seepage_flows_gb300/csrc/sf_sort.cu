@@ -77,22 +77,26 @@ __global__ void __launch_bounds__(kSortThreads) kKeysHist(const SceneDev* __rest
     for (int q = 0; q < kPer; ++q) h[threadIdx.x * kPer + q] = 0;
     __syncthreads();
     const int base = blockIdx.x * kTile;
-    // all of the thread's positions are loaded before the first key
-    float4 p[kSortItems];
-    int sid[kSortItems];
+    // positions are loaded in groups of (up to) four before their keys
+    constexpr int kGroup = kSortItems < 4 ? kSortItems : 4;
+#pragma unroll 1
+    for (int r0 = 0; r0 < kSortItems; r0 += kGroup) {
+        float4 p[kGroup];
+        int sid[kGroup];
 #pragma unroll
-    for (int r = 0; r < kSortItems; ++r) {
-        const int slot = base + r * kSortThreads + threadIdx.x;
-        sid[r] = slot < n ? blockScene[slot / kSlotAlign] : 0;
-        p[r] = slot < n ? pos4[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
+        for (int u = 0; u < kGroup; ++u) {
+            const int slot = base + (r0 + u) * kSortThreads + threadIdx.x;
+            sid[u] = slot < n ? blockScene[slot / kSlotAlign] : 0;
+            p[u] = slot < n ? pos4[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
 #pragma unroll
-    for (int r = 0; r < kSortItems; ++r) {
-        const int slot = base + r * kSortThreads + threadIdx.x;
-        if (slot < n) {
-            const unsigned int k = slotKey(scenes[sid[r]], p[r], errWord);
-            keys[slot] = k;
-            atomicAdd(&h[k & unsigned(R - 1)], 1u);
+        for (int u = 0; u < kGroup; ++u) {
+            const int slot = base + (r0 + u) * kSortThreads + threadIdx.x;
+            if (slot < n) {
+                const unsigned int k = slotKey(scenes[sid[u]], p[u], errWord);
+                keys[slot] = k;
+                atomicAdd(&h[k & unsigned(R - 1)], 1u);
+            }
         }
     }
     __syncthreads();
@@ -135,33 +139,29 @@ void launchKeysHist(const LaunchCtx& c, int n, const float4* pos4, unsigned int*
     }
 }
 
-// Per-digit exclusive scan over tiles, one warp per digit: warp d scans
-// hist[d * tiles .. d * tiles + tiles) in place, 32 tiles per step with
-// shuffles (the next 32 counts are loaded before the current ones are
-// scanned), and writes the digit's total.
-constexpr int kScanWarps = 8;
-__global__ void __launch_bounds__(kScanWarps * 32) kScanTiles(unsigned int* __restrict__ hist, int tiles,
-                                                              unsigned int* __restrict__ digitTotal, int digits) {
-    const int d = blockIdx.x * kScanWarps + int(threadIdx.x >> 5);
-    if (d >= digits) return;  // whole warps
-    const int lane = int(threadIdx.x & 31u);
-    unsigned int* h = hist + size_t(d) * tiles;
+// Per-digit exclusive scan over tiles: block d scans hist[d * tiles ..
+// d * tiles + tiles) in place and writes the digit's total.
+__global__ void __launch_bounds__(kSortThreads) kScanTiles(unsigned int* __restrict__ hist, int tiles,
+                                                           unsigned int* __restrict__ digitTotal) {
+    __shared__ unsigned int part[kSortThreads];
+    unsigned int* h = hist + size_t(blockIdx.x) * tiles;
     unsigned int carry = 0;
-    unsigned int next = lane < tiles ? h[lane] : 0u;
-    for (int base = 0; base < tiles; base += 32) {
-        const unsigned int v = next;
-        const int t = base + lane;
-        next = t + 32 < tiles ? h[t + 32] : 0u;
-        unsigned int incl = v;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned int u = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += u;
+    for (int base = 0; base < tiles; base += kSortThreads) {
+        const int t = base + threadIdx.x;
+        const unsigned int v = t < tiles ? h[t] : 0u;
+        part[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < kSortThreads; o <<= 1) {
+            const unsigned int u = threadIdx.x >= o ? part[threadIdx.x - o] : 0u;
+            __syncthreads();
+            part[threadIdx.x] += u;
+            __syncthreads();
         }
-        if (t < tiles) h[t] = carry + incl - v;
-        carry += __shfl_sync(0xffffffffu, incl, 31);
+        if (t < tiles) h[t] = carry + part[threadIdx.x] - v;
+        carry += part[kSortThreads - 1];
+        __syncthreads();
     }
-    if (lane == 0) digitTotal[d] = carry;
+    if (threadIdx.x == 0) digitTotal[blockIdx.x] = carry;
 }
 
 template <int kSortItems, int kBits>
@@ -251,8 +251,7 @@ static void launchPassT(cudaStream_t s, int n, int shift, const unsigned int* kI
                         unsigned int* kOut, unsigned int* vOut, const SortScratch& sc, bool histDone) {
     const int tiles = sc.tiles;
     if (!histDone) kHist<kSortItems, kBits><<<tiles, kSortThreads, 0, s>>>(kIn, n, shift, sc.hist, tiles);
-    kScanTiles<<<((1 << kBits) + kScanWarps - 1) / kScanWarps, kScanWarps * 32, 0, s>>>(sc.hist, tiles, sc.digitTotal,
-                                                                                       1 << kBits);
+    kScanTiles<<<1 << kBits, kSortThreads, 0, s>>>(sc.hist, tiles, sc.digitTotal);
     kScatter<kSortItems, kBits><<<tiles, kSortThreads, 0, s>>>(kIn, vIn, kOut, vOut, n, shift, sc.hist, tiles,
                                                                sc.digitTotal);
 }
