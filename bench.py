@@ -430,6 +430,7 @@ def run_ours(args, rank, world):
     lab = sim.field("label")
     pairs = int(4 * nbrs[lab == 0].sum() + 3 * nbrs[lab == 1].sum())
     bgeo = None if args.no_bgeo else bgeo_export_timing(sim, n)
+    frame = None if args.no_frame else frame_timing(sim, n)
     batched = None if args.no_batched else batched_comparison(stream)
     adjoint = None if args.no_adjoint else adjoint_comparison(stream)
     calib = None if args.no_calibration else calibration_timing(stream)
@@ -461,12 +462,30 @@ def run_ours(args, rank, world):
         "clocks": clk,
         "e2e": e2e,
         "bgeo_export": bgeo,
+        "frame_adaptive": frame,
         "cpu_baseline": cpu,
         "batched": batched,
         "adjoint": adjoint,
         "calibration": calib,
     }
     print(json.dumps(line), flush=True)
+
+
+def frame_timing(sim, n, frames=2):
+    """The reference app's frame loop (sf_frame_adaptive, main.cpp:240-247):
+    CFL substeps until 1/30 s has passed, each substep followed by the read of
+    its substep count that the loop needs. Wall time over `frames` frames
+    after one untimed frame, on the state the other measurements left."""
+    interval = 1.0 / 30.0
+    sim.frame_adaptive(interval)
+    sim.synchronize()
+    t0 = time.perf_counter()
+    substeps = sum(sim.frame_adaptive(interval) for _ in range(frames))
+    sim.synchronize()
+    el = time.perf_counter() - t0
+    return {"frames": frames, "substeps": substeps, "ms_per_substep": el / substeps * 1e3,
+            "value": n * substeps / el, "unit": "particle-substeps/s",
+            "path": "sf_frame_adaptive(1/30 s): sf_step per substep, N_sub read back after each"}
 
 
 def bgeo_export_timing(sim, n):
@@ -505,6 +524,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-calibration", action="store_true")
     ap.add_argument("--no-bgeo", action="store_true")
+    ap.add_argument("--no-frame", action="store_true")
     ap.add_argument("--adjoint-substeps", type=int, default=0,
                     help="only time the gradient run of the workload over this many substeps")
     ap.add_argument("--checkpoint-every", type=int, default=0,

@@ -219,6 +219,11 @@ struct sf_handle {
     int64_t launches = 0;
     GraphCache graph[2];   // two-substep graphs, by starting buffer set
     GraphCache graph1[2];  // one-substep graphs, by starting buffer set
+    // sf_step's adaptive substep, by starting buffer set: the integrator reads
+    // the render interval from dTimeArg, written before each replay
+    GraphCache graphStep[2];
+    float* dTimeArg = nullptr;
+    bool captureStep = false;  // runStage passes dTimeArg to the integrator while capturing graphStep
     int nbrCap = kMinNbr;                 // particle neighbour list capacity (per slot)
     // list growth: copies of the scene states queued behind the substeps and
     // read once they have landed (pinned, n_scenes each; two in flight at most)
@@ -309,6 +314,12 @@ struct sf_handle {
     }
     // Drop the captured substep graphs (after a change of buffers or launch shapes).
     void dropGraphs() {
+        for (auto& g : graphStep) {
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+            g.dt = 0.f;
+            g.nodes = 0;
+        }
         for (auto& g : graph1) {
             if (g.exec) cudaGraphExecDestroy(g.exec);
             g.exec = nullptr;
@@ -336,6 +347,9 @@ struct sf_handle {
             if (g.exec) cudaGraphExecDestroy(g.exec);
         for (auto& g : graph1)
             if (g.exec) cudaGraphExecDestroy(g.exec);
+        for (auto& g : graphStep)
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+        devFree(dTimeArg);
         devFree(dProbe);
         for (int k = 0; k < 2; ++k) {
             if (stateHost[k]) cudaFreeHost(stateHost[k]);
@@ -421,7 +435,7 @@ sf_status runStage(sf_handle* h, int stage, float timeArg, int adaptive) {
     case SF_STAGE_VOIDAGE_ADHESION: launchVoidageAdhesion(c, b); break;
     case SF_STAGE_SAND_MOMENTUM: launchSandMomentum(c, b); break;
     case SF_STAGE_WATER_MOMENTUM: launchWaterMomentum(c, b); break;
-    case SF_STAGE_INTEGRATE: launchIntegrate(c, b, timeArg, adaptive); break;
+    case SF_STAGE_INTEGRATE: launchIntegrate(c, b, timeArg, adaptive, h->captureStep ? h->dTimeArg : nullptr); break;
     default: return h->fail(SF_ERR_INVALID, "unknown stage");
     }
     h->launches += 1;
@@ -701,6 +715,7 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
     SF_ALLOC(h->dState, sizeof(SceneState) * n_scenes);
     SF_ALLOC(h->dErr, sizeof(unsigned));
     SF_ALLOC(h->dProbe, sizeof(unsigned));
+    SF_ALLOC(h->dTimeArg, sizeof(float));
 #undef SF_ALLOC
     for (int k = 0; k < 2; ++k)
         if (h->cuda(cudaMallocHost(reinterpret_cast<void**>(&h->stateHost[k]), sizeof(SceneState) * n_scenes),
@@ -827,6 +842,33 @@ sf_status sf_run_stage(sf_handle* h, int32_t stage, float time_arg, int32_t adap
     return runStage(h, stage, time_arg, adaptive);
 }
 
+// sf_step's adaptive substep as a graph starting from buffer set h->cur,
+// captured on first use: the integrator reads the render interval from
+// h->dTimeArg, which sf_step writes before each replay.
+static sf_status ensureStepGraph(sf_handle* h, GraphCache& g) {
+    if (g.exec) return SF_OK;
+    const int curBefore = h->cur;
+    const int64_t launchesBefore = h->launches;
+    cudaGraph_t graph = nullptr;
+    sf_status st = h->cuda(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    if (st) return st;
+    h->captureStep = true;
+    st = runSubstep(h, 0.f, 1);
+    h->captureStep = false;
+    const cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+    h->cur = curBefore;
+    g.nodes = int(h->launches - launchesBefore);
+    h->launches = launchesBefore;
+    if (st != SF_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return st;
+    }
+    if (h->cuda(ce, "end capture")) return SF_ERR_CUDA;
+    st = h->cuda(cudaGraphInstantiate(&g.exec, graph, 0), "graph instantiate");
+    cudaGraphDestroy(graph);
+    return st;
+}
+
 sf_status sf_step(sf_handle* h, float render_interval, int64_t* n_substeps_out, float* ms_out) {
     if (!h) return SF_ERR_INVALID;
     if (sf_status gs = growListsIfFull(h, -1)) return gs;
@@ -836,8 +878,19 @@ sf_status sf_step(sf_handle* h, float render_interval, int64_t* n_substeps_out, 
         cudaEventCreate(&e1);
         cudaEventRecord(e0, h->stream);
     }
-    sf_status st = runSubstep(h, render_interval, 1);
+    // the substep is replayed from a captured graph; its render interval goes
+    // to the device first (a pageable source: the copy is staged before the
+    // call returns)
+    const float t = render_interval;
+    if (h->cuda(cudaMemcpyAsync(h->dTimeArg, &t, sizeof(float), cudaMemcpyHostToDevice, h->stream), "step time"))
+        return SF_ERR_CUDA;
+    GraphCache& g = h->graphStep[h->cur];
+    sf_status st = ensureStepGraph(h, g);
     if (st != SF_OK) return st;
+    if (h->cuda(cudaGraphLaunch(g.exec, h->stream), "graph launch")) return SF_ERR_CUDA;
+    h->launches += g.nodes;
+    h->cur = 1 - h->cur;
+    h->sorted = true;
     queueStateCopy(h);
     if (ms_out) {
         cudaEventRecord(e1, h->stream);

@@ -915,11 +915,13 @@ __device__ __forceinline__ long long cflSubsteps(const SceneDev& S, float amax, 
 }
 
 __global__ void kIntegrate(const SceneDev* __restrict__ scenes, const int* __restrict__ blockScene,
-                           SceneState* __restrict__ state, float timeArg, int adaptive,
+                           SceneState* __restrict__ state, float timeArg, const float* __restrict__ timeArgDev,
+                           int adaptive,
                            const unsigned int* __restrict__ bcs, const float4* __restrict__ bpos4,
                            float4* __restrict__ pos4, float4* __restrict__ vel4, float4* __restrict__ acc4,
                            float4* __restrict__ adh4, float4* __restrict__ avgadh4) {
     SF_SLOT_PROLOGUE
+    if (timeArgDev) timeArg = *timeArgDev;  // a graph-replayed step reads the time from the device
     float dt = timeArg;
     if (adaptive) {
         const long long ns = cflSubsteps(S, __uint_as_float(state[sid].amax_bits), timeArg);
@@ -1093,8 +1095,9 @@ void launchWaterMomentum(const LaunchCtx& c, const PassBuffers& b) {
     }
 }
 
-void launchIntegrate(const LaunchCtx& c, const PassBuffers& b, float timeArg, int adaptive) {
-    kIntegrate<<<grid(c, kPassIntegrate), c.block[kPassIntegrate], 0, c.stream>>>(c.scenes, c.blockScene, c.state, timeArg, adaptive,
+void launchIntegrate(const LaunchCtx& c, const PassBuffers& b, float timeArg, int adaptive, const float* timeArgDev) {
+    kIntegrate<<<grid(c, kPassIntegrate), c.block[kPassIntegrate], 0, c.stream>>>(c.scenes, c.blockScene, c.state,
+                                                          timeArg, timeArgDev, adaptive,
                                                           b.lists.bcs, b.bpos4, b.pos4, b.vel4, b.acc4, b.adh4,
                                                           b.avgadh4);
 }

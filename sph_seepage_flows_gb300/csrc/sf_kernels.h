@@ -113,7 +113,10 @@ void launchAvgFlow(const LaunchCtx& c, const PassBuffers& b);
 void launchVoidageAdhesion(const LaunchCtx& c, const PassBuffers& b);
 void launchSandMomentum(const LaunchCtx& c, const PassBuffers& b);
 void launchWaterMomentum(const LaunchCtx& c, const PassBuffers& b);
-void launchIntegrate(const LaunchCtx& c, const PassBuffers& b, float timeArg, int adaptive);
+// timeArgDev: when not null, the kernel reads timeArg from this device scalar
+// (graph-replayed steps whose render interval changes from call to call).
+void launchIntegrate(const LaunchCtx& c, const PassBuffers& b, float timeArg, int adaptive,
+                     const float* timeArgDev = nullptr);
 // Largest number of particles within the interaction reach of any particle
 // (itself included), atomically maxed into *maxCount; needs the cell table.
 void launchNeighborCountMax(const LaunchCtx& c, const float4* pos4, const unsigned int* cs, unsigned int* maxCount);
