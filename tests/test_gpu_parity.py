@@ -9,8 +9,8 @@ must be bit-exact. Floating-point results are compared with the norm-relative
 error |gpu - ref| / scale, scale = the per-particle magnitude of the quantity
 (for acceleration: the sum of the magnitudes of all terms added to it, from
 the FP64 oracle; for pressure: stiff * (rho/rho0)^7), with a floor of 1e-3 of
-the field's largest scale. The bar is 1e-5 (the tolerance of the north-star
-requirement "forces within 1e-5 relative of the reference FP32 path"). Fields
+the field's largest scale. The bar is 1e-5: forces within 1e-5 relative of
+the reference's FP32 path. Fields
 computed without transcendental functions must match the FP32 oracle
 bit-for-bit when the inputs are identical.
 """
