@@ -55,7 +55,7 @@ enum {
     SF_ERR_CAPACITY = 3,    /* particle count would exceed the capacity */
     SF_ERR_DEVICE = 4,      /* the device error word is set (see sf_check_error) */
     SF_ERR_NO_DEVICE = 5,   /* no CUDA device is visible */
-    SF_ERR_UNSUPPORTED = 6  /* request not supported by this build */
+    SF_ERR_UNSUPPORTED = 6  /* request not supported by the library */
 };
 
 /* CudaSphSolverType (include/kiri_pbs_cuda/data/cuda_sph_params.h:19-24) */
