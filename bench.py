@@ -59,9 +59,23 @@ STAGE_BYTES = {
 BYTES_PER_SUBSTEP = sum(STAGE_BYTES.values())  # 753
 
 # DRAM bytes (read + write) per launch of each stage's main kernel on the 1M
-# workload, from the committed ncu capture (profiles/neighbor_passes_1M_ncu.md).
-NCU_TRAFFIC = {"density": 283.9e6, "avgflow": 137.1e6, "water_momentum": 139.3e6,
-               "sand_momentum": 65.8e6, "voidage_adhesion": 65.0e6}
+# workload, from one ncu capture, tagged with the digest of the kernel sources
+# it was taken on (csrc_digest()). When the sources have changed since, the
+# figure no longer describes the running kernels and is reported as null.
+NCU_TRAFFIC_DIGEST = ""
+NCU_TRAFFIC = {}
+
+
+def csrc_digest() -> str:
+    """sha256 (first 12 hex digits) of the CUDA sources, in name order."""
+    import hashlib
+    d = hashlib.sha256()
+    csrc = os.path.join(ROOT, "sph_seepage_flows_gb300", "csrc")
+    for name in sorted(os.listdir(csrc)):
+        if name.endswith((".cu", ".cuh", ".h")):
+            with open(os.path.join(csrc, name), "rb") as f:
+                d.update(name.encode() + b"\0" + f.read())
+    return d.hexdigest()[:12]
 
 
 def peaks():
@@ -293,7 +307,44 @@ def calibration_timing(stream, iterations=2, n_substeps=500, checkpoint_every=25
             "wall_ms_per_iteration": float(np.median([m["wall"] for m in ms])),
             "particle_substeps_per_s_forward_and_reverse":
                 float(sum(s.n for s in scs) * n_substeps / (np.median([m["forward"] + m["reverse"] for m in ms]) * 1e-3)),
-            "loss_mean_by_iteration": [float(np.mean(l)) for l in h["loss"]]}
+            "loss_mean_by_iteration": [float(np.mean(l)) for l in h["loss"]],
+            "nonfinite_gradient_scenes_by_iteration": h.get("nonfinite_gradients", [])}
+
+
+def long_run(stream, workload="plain_large", substeps=2000, window=200):
+    """The whole configured run of the workload: `substeps` graph-replayed
+    substeps at the reference dt from the initial state, timed per window of
+    `window` substeps (CUDA events on the library's stream). The state
+    evolves (the seepage front advances and the neighbour lists grow), so
+    later windows cost more than the first; the list capacity is read after
+    each window."""
+    import torch
+
+    from sph_seepage_flows_gb300 import capi
+    sc = make_scene(workload)
+    dt = reference_dt(sc)
+    sim = capi.Simulation(sc, stream=stream.cuda_stream)
+    tuning = sim.autotune(dt)
+    windows = []
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    total_ms = 0.0
+    for w in range(substeps // window):
+        ev[0].record(stream)
+        sim.substeps_fixed(dt, window)
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        ms = ev[0].elapsed_time(ev[1])
+        total_ms += ms
+        cap, growths = sim.list_capacity()
+        windows.append({"substeps": [w * window, (w + 1) * window], "ms_per_substep": ms / window,
+                        "list_capacity": cap, "list_growths": growths})
+    flags = sim.check_error()
+    done = window * len(windows)
+    sim.close()
+    return {"workload": workload, "particles": sc.n, "substeps": done, "dt": dt,
+            "mean_ms_per_substep": total_ms / done, "value": sc.n * done / (total_ms * 1e-3),
+            "unit": "particle-substeps/s", "windows": windows, "device_error_flags": flags,
+            "list_capacity_initial": tuning["list_capacity"]}
 
 
 def run_reference(args, rank, world):
@@ -385,6 +436,11 @@ def run_ours(args, rank, world):
             stage_ms[s] += evs[k].elapsed_time(evs[k + 1]) / reps
     top = max(stage_ms, key=stage_ms.get)
     peak, peak_kind = peaks()
+    digest = csrc_digest()
+    traffic, traffic_source = None, "no ncu capture of the current kernel sources"
+    if args.workload == "plain_large" and digest == NCU_TRAFFIC_DIGEST and top in NCU_TRAFFIC:
+        traffic = NCU_TRAFFIC[top]
+        traffic_source = f"ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, sources {digest}"
     achieved = STAGE_BYTES[top] * n / (stage_ms[top] * 1e-3) / 1e9
 
     # e2e through the C ABI with pinned host buffers
@@ -434,6 +490,7 @@ def run_ours(args, rank, world):
     batched = None if args.no_batched else batched_comparison(stream)
     adjoint = None if args.no_adjoint else adjoint_comparison(stream)
     calib = None if args.no_calibration else calibration_timing(stream)
+    longrun = None if args.no_long_run else long_run(stream, args.workload)
     if rank != 0:
         return
     cpu = None if args.no_cpu else cpu_baseline(sc, dt)
@@ -449,8 +506,8 @@ def run_ours(args, rank, world):
                    "parallelism": f"replicas x{world}", "tuning": tuning},
         "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": NCU_TRAFFIC.get(top) if args.workload == "plain_large" else None,
-                     "traffic_source": "profiles/neighbor_passes_1M_ncu.md (dram read + write per launch)",
+                     "traffic": traffic,
+                     "traffic_source": traffic_source,
                      "algorithmic_bytes_per_particle": STAGE_BYTES[top]},
         "substep_roofline_frac": BYTES_PER_SUBSTEP * n / (ms / steps * 1e-3) / 1e9 / peak,
         "stage_ms": stage_ms,
@@ -467,6 +524,7 @@ def run_ours(args, rank, world):
         "batched": batched,
         "adjoint": adjoint,
         "calibration": calib,
+        "long_run": longrun,
     }
     print(json.dumps(line), flush=True)
 
@@ -525,6 +583,7 @@ def main():
     ap.add_argument("--no-calibration", action="store_true")
     ap.add_argument("--no-bgeo", action="store_true")
     ap.add_argument("--no-frame", action="store_true")
+    ap.add_argument("--no-long-run", action="store_true")
     ap.add_argument("--adjoint-substeps", type=int, default=0,
                     help="only time the gradient run of the workload over this many substeps")
     ap.add_argument("--checkpoint-every", type=int, default=0,

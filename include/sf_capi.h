@@ -387,12 +387,15 @@ sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t che
  *   cell_start_out_dev  out: G + 1 ints, device, G = grid cells:
  *                            first sorted index with cell >= c; entry G = n
  *   stream              the CUDA stream to use (NULL = the legacy default stream)
- * The call waits for its stream before returning (it reads back a flag) and
- * returns SF_ERR_DEVICE when a position is not finite. The first call on a
+ * Every call copies a flag word to host memory and waits for its stream
+ * before returning, and returns SF_ERR_DEVICE when a position is not finite;
+ * the output buffers then hold unspecified values. The first call on a
  * device looks up the scratch address (cudaGetSymbolAddress), which may load
- * the module: make the first call before any stream capture. Calls that
- * overlap on the GPU (two streams or host threads) share the scratch and
- * race: serialise them. Errors are reported by sf_last_error_string(NULL). */
+ * the module: make the first call before any stream capture. The lookup is
+ * repeated when the cached address no longer belongs to the device (after
+ * cudaDeviceReset). Calls that overlap on the GPU (two streams or host
+ * threads) share the scratch and race: serialise them. Errors are reported
+ * by sf_last_error_string(NULL). */
 #define SF_NOALLOC_MAX_PARTICLES 262144
 sf_status sf_cell_sort_noalloc(const sf_boundary_params* grid, const float* pos_dev, int64_t n,
                                int32_t* perm_out_dev, int32_t* cell_start_out_dev, void* stream);

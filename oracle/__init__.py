@@ -1,10 +1,13 @@
 """ORACLE -- test infrastructure, not product code.
 
-ctypes wrappers of the CPU oracle (oracle/sf_oracle.cpp -> oracle/libsforacle.so)
-and of the reference harness (oracle/ref_harness.cpp -> oracle/_ref/libsfref.so,
-built only where the reference sources are mounted). Only tests/,
-__graft_entry__.smoke() and bench.py's CPU-baseline leg use this package, and
-only as the checker of the CUDA path.
+ctypes wrappers of the CPU oracle (oracle/sf_oracle.cpp -> oracle/libsforacle.so),
+of the reference harness (oracle/ref_harness.cpp -> oracle/_ref/libsfref.so,
+built only where the reference sources are mounted) and of the reference's
+own CUDA library driven through its public classes (oracle/ref_gpu_driver.cu
+-> baseline/_ref/libsfrefgpu.so, built by oracle/build_ref_cuda.sh from the
+staged reference sources). Only tests/, __graft_entry__.smoke() and bench.py's
+baseline legs use this package, and only as the checker of the CUDA path or
+as the baseline it is timed against.
 """
 
 from __future__ import annotations
@@ -21,6 +24,7 @@ from sph_seepage_flows_gb300.params import BFIELDS, FIELDS, STAGE_ID, SfBoundary
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "libsforacle.so")
 REF_SO = os.path.join(HERE, "_ref", "libsfref.so")
+REF_GPU_SO = os.path.join(os.path.dirname(HERE), "baseline", "_ref", "libsfrefgpu.so")
 
 
 def build(force: bool = False) -> str:
@@ -35,6 +39,13 @@ def build_ref() -> str | None:
     """Compile the reference harness when the reference sources are present."""
     subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")], check=True)
     return REF_SO if os.path.exists(REF_SO) else None
+
+
+def build_ref_gpu() -> str | None:
+    """Stage (where the reference sources are mounted) and compile (where the
+    staged copy exists) the reference's CUDA library with its driver."""
+    subprocess.run(["sh", os.path.join(HERE, "build_ref_cuda.sh")], check=True)
+    return REF_GPU_SO if os.path.exists(REF_GPU_SO) else None
 
 
 def _fptr(a):
@@ -340,4 +351,108 @@ def ref_emitter_points(pos, vel, kind, particle_radius, r_or_w, h=0.0):
     out = np.zeros((n, 3), np.float32)
     lib.sfref_emitter_points(_fptr(p), _fptr(v), int(kind), float(particle_radius), float(r_or_w), float(h),
                              _fptr(out), n)
+    return out
+
+
+_REF_GPU_LIB = None
+
+
+def ref_gpu_lib():
+    """The reference's CUDA library with its driver, or None where it was not built."""
+    global _REF_GPU_LIB
+    if _REF_GPU_LIB is None and os.path.exists(REF_GPU_SO):
+        lib = ctypes.CDLL(REF_GPU_SO)
+        lib.sfrg_create.restype = ctypes.c_void_p
+        lib.sfrg_create.argtypes = [ctypes.POINTER(SfParams), ctypes.POINTER(SfBoundaryParams),
+                                    ctypes.POINTER(SfSolverParams), ctypes.POINTER(SfSceneInit), ctypes.c_int64,
+                                    ctypes.c_int]
+        lib.sfrg_destroy.argtypes = [ctypes.c_void_p]
+        lib.sfrg_update.restype = ctypes.c_float
+        lib.sfrg_update.argtypes = [ctypes.c_void_p, ctypes.c_float]
+        lib.sfrg_run.restype = ctypes.c_double
+        lib.sfrg_run.argtypes = [ctypes.c_void_p, ctypes.c_float, ctypes.c_int64]
+        lib.sfrg_num_substeps.restype = ctypes.c_int64
+        lib.sfrg_num_substeps.argtypes = [ctypes.c_void_p]
+        lib.sfrg_size.restype = ctypes.c_int64
+        lib.sfrg_size.argtypes = [ctypes.c_void_p]
+        lib.sfrg_get_field.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                       ctypes.c_int64]
+        lib.sfrg_get_cell_table.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int64),
+                                            ctypes.c_int64]
+        _REF_GPU_LIB = lib
+    return _REF_GPU_LIB
+
+
+class RefGpu(_Base):
+    """The reference's own CUDA library (-use_fast_math, its kernels and
+    Thrust calls) driven through its public classes: each step is one
+    CudaBaseSystem::UpdateSystem(render_interval) call."""
+
+    _prefix = "sfrg_"
+
+    def __init__(self, scene, capacity=None, sort_multi: int = 1):
+        self._lib = ref_gpu_lib()
+        if self._lib is None:
+            raise RuntimeError("reference CUDA library not built (baseline/_ref/libsfrefgpu.so)")
+        self.params, self.bparams, self.sparams = scene.params, scene.bparams, scene.sparams
+        self._init = SceneInit(scene)
+        self.n, self.nb = scene.n, scene.nb
+        self.h = self._lib.sfrg_create(ctypes.byref(self.params), ctypes.byref(self.bparams),
+                                       ctypes.byref(self.sparams), ctypes.byref(self._init.init),
+                                       ctypes.c_int64(capacity or scene.n), int(sort_multi))
+        if not self.h:
+            raise RuntimeError("the reference CUDA library failed to build the system")
+
+    def update(self, render_interval: float) -> float:
+        """One UpdateSystem call; returns the reference's own event-timed ms."""
+        return float(self._lib.sfrg_update(self.h, float(render_interval)))
+
+    def run(self, render_interval: float, calls: int) -> float:
+        """`calls` UpdateSystem calls; wall milliseconds of all of them."""
+        return float(self._lib.sfrg_run(self.h, float(render_interval), ctypes.c_int64(calls)))
+
+    @property
+    def num_substeps(self) -> int:
+        return int(self._lib.sfrg_num_substeps(self.h))
+
+
+PARTIO_SO = os.path.join(HERE, "_ref", "libpartioref.so")
+_PARTIO_LIB = None
+
+
+def partio_lib():
+    """partio's own .bgeo writer / reader (oracle/partio_harness.cpp), or None
+    where the reference sources were not mounted to build it."""
+    global _PARTIO_LIB
+    if _PARTIO_LIB is None and os.path.exists(PARTIO_SO):
+        lib = ctypes.CDLL(PARTIO_SO)
+        F = ctypes.POINTER(ctypes.c_float)
+        lib.sfpartio_write.restype = ctypes.c_int
+        lib.sfpartio_write.argtypes = [ctypes.c_char_p, F, F, F, ctypes.POINTER(ctypes.c_int64), ctypes.c_int64]
+        lib.sfpartio_read.restype = ctypes.c_int64
+        lib.sfpartio_read.argtypes = [ctypes.c_char_p, F, ctypes.c_int64, ctypes.c_int]
+        _PARTIO_LIB = lib
+    return _PARTIO_LIB
+
+
+def partio_write(path, pos, col, radius, label) -> None:
+    """The reference's ExportBgeoFileCUDA particle set written by partio."""
+    lib = partio_lib()
+    p = np.ascontiguousarray(pos, np.float32)
+    c = np.ascontiguousarray(col, np.float32)
+    r = np.ascontiguousarray(radius, np.float32)
+    lab = np.ascontiguousarray(label, np.int64)
+    if lib.sfpartio_write(str(path).encode(), _fptr(p), _fptr(c), _fptr(r),
+                          lab.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), len(r)) != 0:
+        raise RuntimeError("partio writeBGEO failed")
+
+
+def partio_read_for_gpu(path, flip_yz: bool = False) -> np.ndarray:
+    """ReadBgeoFileForGPU through partio's reader: (n, 4) x, y, z, pscale."""
+    lib = partio_lib()
+    n = lib.sfpartio_read(str(path).encode(), None, 0, int(flip_yz))
+    if n < 0:
+        raise RuntimeError("partio readBGEO failed")
+    out = np.zeros((n, 4), np.float32)
+    lib.sfpartio_read(str(path).encode(), _fptr(out), n, int(flip_yz))
     return out

@@ -6,10 +6,13 @@ ExportBgeoFileCUDA (seepage_flows/include/kiri_utils.h:364-448) and reads
 in ReadBgeoFileForGPU / ReadMultiBgeoFilesForGPU (kiri_utils.h:252-362).
 Only tests/ use it, as the checker of sf_export_bgeo / sf_read_bgeo.
 
-Parity unpinned: partio is present in the reference only as headers and a
-prebuilt Windows library (extlib/lib/partio.lib, which is not read or run
-here), and the reference holds no .bgeo file. The layout restated here is
-the published classic-bgeo (version 5) point layout as partio uses it:
+Pinned to partio: the reference vendors partio's sources
+(extlib/include/partio; writeBGEO in io/BGEO.cpp), which oracle/build_ref.sh
+compiles in place into oracle/_ref/libpartioref.so. This writer produces
+partio's bytes for the reference's particle set (tests/test_bgeo_partio_cpu.py;
+tests/golden/partio_export.npz carries partio's bytes for a seeded set), and
+its reader and the library's agree with partio's reader. The layout, the
+classic-bgeo (version 5) point layout as partio writes it:
 
   header, big-endian: int32 magic 'Bgeo', char 'V', int32 version 5, then
     int32 counts: points, primitives, point groups, primitive groups, point

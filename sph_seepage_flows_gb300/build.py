@@ -2,10 +2,11 @@
 drop-in facade test program.
 
 Each translation unit is compiled by nvcc in parallel into _build/, then
-linked into sph_seepage_flows_gb300/libsf_gb300.so. The substep passes are
-built with --fmad=false and IEEE division / square root so that their FP32
-arithmetic matches the reference kernels' operation order exactly; the
-adjoint (sf_adjoint.cu) uses the fast intrinsics.
+linked into sph_seepage_flows_gb300/libsf_gb300.so. The passes whose results
+are bit-exact against the reference (sort, density, average flow, voidage /
+adhesion, integrate) are built with --fmad=false and IEEE division / square
+root so that their FP32 arithmetic matches the reference kernels' operation
+order exactly; the adjoint (sf_adjoint.cu) uses the fast intrinsics.
 """
 
 from __future__ import annotations
@@ -21,7 +22,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "libsf_gb300.so")
-SOURCES = ["sf_kernels.cu", "sf_sort.cu", "sf_adjoint.cu", "sf_capi.cu", "sf_noalloc.cu", "sf_bgeo.cu"]
+SOURCES = ["sf_kernels.cu", "sf_momentum.cu", "sf_sort.cu", "sf_adjoint.cu", "sf_capi.cu", "sf_noalloc.cu", "sf_bgeo.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -33,13 +34,21 @@ def nvcc() -> str:
 
 # The forward passes reproduce the reference's FP32 operation order (no
 # contraction, IEEE division and square root). The adjoint only has to be
-# accurate to its gradient tolerance and uses the fast intrinsics.
+# accurate to its gradient tolerance and uses the fast intrinsics. The
+# momentum passes (sf_momentum.cu) keep the forward arithmetic too: with
+# multiply-add contraction the compiler contracts the list walk and the
+# overflow stencil walk, into which the same pair term is inlined, in
+# different places, so a particle's force would depend on which path ran.
 PRECISE = ["--fmad=false", "-prec-div=true", "-prec-sqrt=true"]
 FAST_SOURCES = {"sf_adjoint.cu"}
 
 
+def arith_flags(src: str) -> list:
+    return ["-use_fast_math"] if src in FAST_SOURCES else PRECISE
+
+
 def common_flags(src: str = "") -> list:
-    arith = ["-use_fast_math"] if src in FAST_SOURCES else PRECISE
+    arith = arith_flags(src)
     return ARCH + ["-O3", "-std=c++17", "-lineinfo"] + arith + [
         "--extended-lambda", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I", os.path.join(ROOT, "include")]
 

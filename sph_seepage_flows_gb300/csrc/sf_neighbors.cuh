@@ -8,6 +8,17 @@
 
 namespace sfg {
 
+// The lane-split passes run G consecutive threads per slot (G = 1, 2, 4 or 8,
+// chosen per handle by the slot count): lane `part` takes every G-th
+// neighbour and lane 0 adds up the lanes' sums and writes the slot. Their
+// sums are already in a different order from the reference's, so the split
+// only moves FP32 rounding; small scenes get G times the threads in flight.
+#define SF_SLOT_PROLOGUE_G                                                      \
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;                      \
+    const int slot = gid / G, part = gid % G;                                   \
+    const int sid = blockScene[(blockIdx.x * (blockDim.x / G)) / kSlotAlign];   \
+    const SceneDev& S = scenes[sid];
+
 // 27-cell stencil of the reference, with the global cell index of cell m.
 template <typename F>
 __device__ __forceinline__ void forEachCell(const SceneDev& S, int3 c, F&& f) {

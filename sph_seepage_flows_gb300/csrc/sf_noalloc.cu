@@ -5,12 +5,14 @@
 // The scratch (g_noallocScratch) holds the keys, the ping-pong key and
 // permutation buffers, the digit histograms and totals of the radix sort and
 // a non-finite-position flag. Its device address is looked up once per
-// device with cudaGetSymbolAddress (the first call on a device does it), so
-// the call itself issues only kernels, one memset, device-to-device copies
-// and one small device-to-host read. Every histogram and total is written
-// before it is read; the flag is the only word that must start at zero and
-// is cleared by every call. Calls that overlap on the GPU share the scratch
-// and race.
+// device with cudaGetSymbolAddress (the first call on a device does it, and
+// the first call after that device's context was reset, which is detected
+// by asking the runtime whether the cached address is still a device
+// address), so the call itself issues only kernels, one memset,
+// device-to-device copies and one small device-to-host read. Every
+// histogram and total is written before it is read; the flag is the only
+// word that must start at zero and is cleared by every call. Calls that
+// overlap on the GPU share the scratch and race.
 #include "../../include/sf_capi.h"
 #include "sf_device.cuh"
 #include "sf_kernels.h"
@@ -50,7 +52,21 @@ sf_status failWith(sf_status st, const std::string& msg) {
     return st;
 }
 
-// Device address of the scratch on the current device (looked up once per device).
+// Is p still a device address of `device`? After cudaDeviceReset (or any
+// teardown of the primary context) the module is loaded again and a cached
+// address may be stale; the runtime then no longer knows it as device memory.
+bool stillDeviceAddress(const void* p, int device) {
+    cudaPointerAttributes a{};
+    const cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();  // not sticky: clear it so later checks see only their own errors
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice && a.device == device;
+}
+
+// Device address of the scratch on the current device: looked up on the first
+// call on a device and again whenever the cached address went stale.
 unsigned int* scratchAddress(int device, std::string& why) {
     static std::mutex mu;
     static unsigned int* addr[kMaxDevices] = {};
@@ -59,6 +75,7 @@ unsigned int* scratchAddress(int device, std::string& why) {
         why = "device index out of range";
         return nullptr;
     }
+    if (addr[device] && !stillDeviceAddress(addr[device], device)) addr[device] = nullptr;
     if (!addr[device]) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);

@@ -1,8 +1,9 @@
 """The GPU .bgeo export (sf_export_bgeo, sf_export_bgeo_device) against the
-oracle's writer: the files are byte-identical to the oracle's for the same
-particle arrays (the handle's current, cell-sorted order), they read back
-through sf_read_bgeo, and the 1M-particle scene's export parses to exactly
-its fields."""
+oracle's writer and partio's: the files are byte-identical to the oracle's
+for the same particle arrays (the handle's current, cell-sorted order) and to
+the bytes partio's own writer produced for the committed point set
+(tests/golden/partio_export.npz), they read back through sf_read_bgeo, and
+the 1M-particle scene's export parses to exactly its fields."""
 
 import numpy as np
 import pytest
@@ -47,6 +48,18 @@ def test_device_array_export_is_byte_identical(cuda_lib, tmp_path):
         stream = torch.cuda.current_stream().cuda_stream
         export_bgeo_device(str(tmp_path), f"d{n}", *[x.data_ptr() if n else 0 for x in t], n, stream)
         assert (tmp_path / f"d{n}.bgeo").read_bytes() == bgeo.write_bytes(pos, col, rad, lab), n
+
+
+def test_device_array_export_equals_partio_bytes(cuda_lib, tmp_path):
+    import torch
+
+    from helpers import load_golden
+    from sph_seepage_flows_gb300.capi import export_bgeo_device
+    g = load_golden("partio_export.npz")
+    t = [torch.from_numpy(np.ascontiguousarray(g[k])).cuda() for k in ("pos", "col", "radius", "label")]
+    stream = torch.cuda.current_stream().cuda_stream
+    export_bgeo_device(str(tmp_path), "partio", *[x.data_ptr() for x in t], len(g["radius"]), stream)
+    assert (tmp_path / "partio.bgeo").read_bytes() == g["bgeo"].tobytes()
 
 
 def test_large_scene_export_parses_to_its_fields(cuda_lib, tmp_path):

@@ -18,7 +18,7 @@ bit-for-bit when the inputs are identical.
 import numpy as np
 import pytest
 
-from helpers import exact_fraction, load_golden, rel_err, scene_from_golden
+from helpers import compare_stages, exact_fraction, load_golden, rel_err, scene_from_golden
 from sph_seepage_flows_gb300 import scenes
 from sph_seepage_flows_gb300.params import STAGES
 
@@ -114,44 +114,7 @@ def test_stages_bit_exact_against_fp32_oracle(cuda_lib, oracle_mod, which, lanes
     sim = gpu_sim(sc)
     sim.set_lanes(lanes)
     o32 = oracle_mod.Oracle(sc, 32)
-    outputs = {
-        "sort": ["id", "label", "pos", "vel", "col", "mass", "radius", "cda0asat", "amcamcp", "max_saturation"],
-        "density": ["density", "pressure"],
-        "avgflow": ["avg_flow", "voidage", "saturation"],
-        "voidage_adhesion": ["voidage", "adhesion", "avg_adhesion", "col", "max_saturation"],
-        "sand_momentum": ["acc", "avg_drag"],
-        "water_momentum": ["acc"],
-        "integrate": ["pos", "vel", "acc"],
-    }
-    transcendental = {"pressure", "adhesion", "avg_adhesion", "acc", "avg_drag", "pos", "vel"}
-    for rep in range(2 if which == "tiny" else 1):
-        for st in STAGES:
-            sim.stage(st, T_FRAME, adaptive=True)
-            o32.stage(st, T_FRAME, adaptive=True)
-            for name in outputs[st]:
-                got = sim.field(name)
-                ref = o32.field(name)
-                if st == "sand_momentum" and name in ("acc", "avg_drag"):
-                    sand = sim.field("label") == 1
-                    got, ref = got[sand], ref[sand]
-                if st == "water_momentum":
-                    water = sim.field("label") == 0
-                    got, ref = got[water], ref[water]
-                frac = exact_fraction(got, ref)
-                scale = None
-                if name == "acc" and st in ("sand_momentum", "water_momentum"):
-                    # cancelling sums: measure against the sum of term magnitudes
-                    keep = (sim.field("label") == (1 if st == "sand_momentum" else 0))
-                    scale = o32.field("acc_scale")[keep]
-                if name in transcendental:
-                    err = rel_err(got, ref, scale)
-                    assert err <= TOL, (rep, st, name, err)
-                else:
-                    assert frac == 1.0, (rep, st, name, frac, rel_err(got, ref))
-            # continue both from the GPU state so every stage sees identical inputs
-            for name in ("pos", "vel", "acc", "density", "pressure", "voidage", "saturation", "avg_flow",
-                         "avg_drag", "adhesion", "avg_adhesion", "col", "max_saturation"):
-                o32.set_field(name, sim.field(name))
+    compare_stages(sim, o32, T_FRAME, True, TOL, reps=2 if which == "tiny" else 1)
 
 
 def test_fields_set_between_stages_reach_the_momentum_passes(cuda_lib, oracle_mod):
