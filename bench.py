@@ -169,6 +169,32 @@ def cpu_baseline(sc, dt, budget_s=20.0):
                       f"(FP32 CPU restatement of the reference kernels, OpenMP)"}
 
 
+def reference_gpu_baseline(sc, calls=10):
+    """The reference's own CUDA library on the same GPU: seepage_flows_cuda
+    built for sm_103a with its own -use_fast_math flags
+    (oracle/build_ref_cuda.sh) and driven through its public classes
+    (oracle/ref_gpu_driver.cu). Each step is one
+    CudaBaseSystem::UpdateSystem(1/30 s) call on the same scene: one substep
+    of (1/30) / N_sub = the reference dt at rest, ending, as the reference
+    does, with a device synchronisation. Wall time of `calls` calls after one
+    warm-up call (CUDA events around them)."""
+    import oracle
+    try:
+        if oracle.build_ref_gpu() is None:
+            return {"unavailable": "reference CUDA sources not staged (oracle/build_ref_cuda.sh)"}
+    except Exception as e:  # noqa: BLE001 - a baseline leg reports, never aborts the bench
+        return {"unavailable": f"reference CUDA build failed: {e}"[:300]}
+    r = oracle.RefGpu(sc)
+    T = 1.0 / 30.0
+    r.update(T)
+    ms = r.run(T, calls)
+    nsub = r.num_substeps
+    del r
+    return {"value": sc.n * calls / (ms * 1e-3), "unit": "particle-substeps/s", "ms_per_substep": ms / calls,
+            "calls": calls, "n_sub": nsub, "dt": T / nsub,
+            "path": "reference seepage_flows_cuda (-use_fast_math, sm_103a): CudaSFSystem::UpdateSystem(1/30 s)"}
+
+
 def batched_comparison(stream, substeps=100, n_scenes=64, blocks=2):
     """The batched-ensemble workload: n_scenes independent scenes (log-uniform
     2k-60k particles, per-scene friction/capillary/permeability) advanced in
@@ -491,6 +517,7 @@ def run_ours(args, rank, world):
     adjoint = None if args.no_adjoint else adjoint_comparison(stream)
     calib = None if args.no_calibration else calibration_timing(stream)
     longrun = None if args.no_long_run else long_run(stream, args.workload)
+    ref_gpu = None if (args.no_reference_gpu or rank != 0) else reference_gpu_baseline(sc)
     if rank != 0:
         return
     cpu = None if args.no_cpu else cpu_baseline(sc, dt)
@@ -525,6 +552,7 @@ def run_ours(args, rank, world):
         "adjoint": adjoint,
         "calibration": calib,
         "long_run": longrun,
+        "reference_gpu": ref_gpu,
     }
     print(json.dumps(line), flush=True)
 
@@ -584,6 +612,7 @@ def main():
     ap.add_argument("--no-bgeo", action="store_true")
     ap.add_argument("--no-frame", action="store_true")
     ap.add_argument("--no-long-run", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true")
     ap.add_argument("--adjoint-substeps", type=int, default=0,
                     help="only time the gradient run of the workload over this many substeps")
     ap.add_argument("--checkpoint-every", type=int, default=0,

@@ -29,6 +29,7 @@
  *   sf_substeps_fixed    fixed-substep mode of main.cpp:250-258 (no reference counterpart for the graph capture)
  *   sf_create_batched    no reference counterpart (independent scenes in one launch)
  *   sf_adjoint_run       no reference counterpart (reverse-mode gradient of a trajectory loss)
+ *   sf_set_adjoint_seed_scale  no reference counterpart (range of the adjoint's FP32 cotangents)
  *   sf_autotune          no reference counterpart (list capacity and block sizes of the passes)
  *   sf_get_list_capacity no reference counterpart (neighbour list capacity and its growth)
  *
@@ -372,6 +373,18 @@ const char* sf_last_error_string(const sf_handle* h);
 sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t checkpoint_every,
                          const float* target_pos, float* loss_out, float* grad_params_out,
                          float* grad_pos0_out, float* grad_vel0_out, float* ms_out);
+
+/* Seed scale of one scene's adjoint (no reference counterpart). The reverse
+ * sweep of sf_adjoint_run carries its cotangents in FP32, and over long
+ * horizons they grow exponentially (contact and liquid-bridge stiffness,
+ * the stiff Tait pressure) until they overflow. With scale s the scene's
+ * cotangents are seeded with s x dL/dx_T, so every cotangent of the sweep is
+ * s times the unscaled one, and sf_adjoint_run divides s out of the returned
+ * gradients in FP64. A power of two changes no rounding: the gradients equal
+ * the unscaled ones bit for bit wherever neither overflows nor reaches the
+ * subnormal range. scale must be finite and > 0; the default is 1; it is kept
+ * until set again (sf_set_params leaves it). */
+sf_status sf_set_adjoint_seed_scale(sf_handle* h, int32_t scene, float scale);
 
 /* Allocation-free cell sort (no counterpart in the reference; its neighbour
  * searcher allocates its buffers in the CudaGNSearcher constructor).

@@ -146,6 +146,9 @@ def _load_oracle():
         getattr(lib, name).argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                        ctypes.c_int64]
     lib.sfo_seed_param.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    F = ctypes.POINTER(ctypes.c_float)
+    lib.sfo_add_sph_particles.argtypes = [ctypes.c_void_p, F, ctypes.c_int64, F, F, ctypes.c_float, ctypes.c_float,
+                                          ctypes.c_int64]
     return lib
 
 
@@ -213,6 +216,17 @@ class Oracle(_Base):
     def stage(self, name, time_arg: float = 0.0, adaptive: bool = False) -> None:
         sid = STAGE_ID[name] if isinstance(name, str) else int(name)
         self._lib.sfo_run_stage(self.h, sid, float(time_arg), int(adaptive))
+
+    def add_sph_particles(self, pos, col, vel, mass: float, radius: float, capacity: int) -> bool:
+        """AddSphParticles (water); False when Size() + num >= capacity."""
+        p = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+        c = np.ascontiguousarray(col, np.float32)
+        v = np.ascontiguousarray(vel, np.float32)
+        rc = self._lib.sfo_add_sph_particles(self.h, _fptr(p), p.shape[0], _fptr(c), _fptr(v), float(mass),
+                                             float(radius), ctypes.c_int64(capacity))
+        if rc == 0:
+            self.n += p.shape[0]
+        return rc == 0
 
     def substeps(self, time_arg: float, adaptive: bool = False, n: int = 1) -> None:
         self._lib.sfo_substeps(self.h, float(time_arg), int(adaptive), ctypes.c_int64(n))
@@ -365,7 +379,7 @@ def ref_gpu_lib():
         lib.sfrg_create.restype = ctypes.c_void_p
         lib.sfrg_create.argtypes = [ctypes.POINTER(SfParams), ctypes.POINTER(SfBoundaryParams),
                                     ctypes.POINTER(SfSolverParams), ctypes.POINTER(SfSceneInit), ctypes.c_int64,
-                                    ctypes.c_int]
+                                    ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
         lib.sfrg_destroy.argtypes = [ctypes.c_void_p]
         lib.sfrg_update.restype = ctypes.c_float
         lib.sfrg_update.argtypes = [ctypes.c_void_p, ctypes.c_float]
@@ -390,26 +404,48 @@ class RefGpu(_Base):
 
     _prefix = "sfrg_"
 
-    def __init__(self, scene, capacity=None, sort_multi: int = 1):
+    EMIT_TYPES = {"square": 0, "circle": 1, "rectangle": 2}
+
+    def __init__(self, scene, capacity=None, sort_multi: int = 1, emitter=None):
+        """emitter: None, or a dict with pos, vel, col, type ('square',
+        'circle', 'rectangle'), radius, width, height."""
         self._lib = ref_gpu_lib()
         if self._lib is None:
             raise RuntimeError("reference CUDA library not built (baseline/_ref/libsfrefgpu.so)")
         self.params, self.bparams, self.sparams = scene.params, scene.bparams, scene.sparams
         self._init = SceneInit(scene)
         self.n, self.nb = scene.n, scene.nb
+        self._emit = None
+        if emitter is not None:
+            e = emitter
+            self._emit = np.array(list(e["pos"]) + list(e["vel"]) + list(e["col"]) +
+                                  [self.EMIT_TYPES[e.get("type", "square")], e.get("radius", 0.0),
+                                   e.get("width", 0.0), e.get("height", 0.0)], np.float32)
         self.h = self._lib.sfrg_create(ctypes.byref(self.params), ctypes.byref(self.bparams),
                                        ctypes.byref(self.sparams), ctypes.byref(self._init.init),
-                                       ctypes.c_int64(capacity or scene.n), int(sort_multi))
+                                       ctypes.c_int64(capacity or scene.n), int(sort_multi),
+                                       _fptr(self._emit))
         if not self.h:
             raise RuntimeError("the reference CUDA library failed to build the system")
 
     def update(self, render_interval: float) -> float:
         """One UpdateSystem call; returns the reference's own event-timed ms."""
-        return float(self._lib.sfrg_update(self.h, float(render_interval)))
+        ms = float(self._lib.sfrg_update(self.h, float(render_interval)))
+        self.n = int(self._lib.sfrg_size(self.h))
+        return ms
+
+    def boundary_keys(self) -> np.ndarray:
+        out = np.zeros(self.nb, dtype=np.float64)
+        if self._lib.sfrg_get_field(self.h, 35, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                    ctypes.c_int64(self.nb)) != 0:
+            raise RuntimeError("boundary keys")
+        return out.astype(np.int64)
 
     def run(self, render_interval: float, calls: int) -> float:
         """`calls` UpdateSystem calls; wall milliseconds of all of them."""
-        return float(self._lib.sfrg_run(self.h, float(render_interval), ctypes.c_int64(calls)))
+        ms = float(self._lib.sfrg_run(self.h, float(render_interval), ctypes.c_int64(calls)))
+        self.n = int(self._lib.sfrg_size(self.h))
+        return ms
 
     @property
     def num_substeps(self) -> int:

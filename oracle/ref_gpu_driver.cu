@@ -6,16 +6,23 @@
 // (seepage_flows/src/main.cpp:173-220 construction, :244/:257 UpdateSystem,
 // the Get*Ptr getters): the global parameter structs are set, then
 // CudaSFParticles, CudaBoundaryParticles, CudaGNSearcher,
-// CudaGNBoundarySearcher, the WCSPH or SPH seepage solver, a disabled
-// CudaEmitter and CudaSFSystem are constructed, and every step is one
-// CudaBaseSystem::UpdateSystem(renderInterval) call (one substep of
-// renderInterval / N_sub, N_sub from the CFL of the previous substep).
+// CudaGNBoundarySearcher, the WCSPH or SPH seepage solver, a CudaEmitter
+// (disabled unless one is described) and CudaSFSystem are constructed, and
+// every step is one CudaBaseSystem::UpdateSystem(renderInterval) call (one
+// substep of renderInterval / N_sub, N_sub from the CFL of the previous
+// substep).
 //
 // Particle ids: the per-particle radius array is carried through the sort
 // (cuda_neighbor_searcher.cu:81,100) and read by no kernel of the solver
 // (the DEM uses the uniform dem_particle_radius), so the driver stores each
 // particle's creation index in it (exact in float below 2^24) and reads it
 // back as the id; the reference's code is unchanged.
+//
+// Emitter: sfrg_create takes an optional emitter description (position,
+// velocity, colour, type, radius, width, height); the driver then sets
+// CUDA_SPH_EMITTER_PARAMS (enable, run) and hands the system an enabled
+// CudaEmitter, whose samples the system constructor builds
+// (cuda_sf_system.cu:46-70) and whose schedule OnUpdateSolver runs.
 //
 // C ABI for oracle/__init__.py (ctypes); results are copied to host doubles.
 #include "sf_capi.h"
@@ -43,6 +50,7 @@ struct RefGpu {
     size_t cells = 0;
     CudaSeepageflowParams P{};
     CudaBoundaryParams B{};
+    CudaSphEmitterParams E{};
 };
 
 float3 f3(const float* v) { return make_float3(v[0], v[1], v[2]); }
@@ -56,9 +64,17 @@ template <typename T> bool copyDown(std::vector<T>& h, const T* d, size_t n) {
 
 extern "C" {
 
+// Cell keys of the last sort in the current (sorted) order: the searchers
+// sort a copy of the particles' cell keys (mGridIdxArray,
+// cuda_neighbor_searcher.cu:70-111; particle2cell keeps the order before the
+// sort), whose first Size() entries are the sorted keys.
+enum { kFieldKey = SF_FIELD_KEY, kBFieldKey = 35 };
+
 // Creates the reference system for one scene; null on a CUDA error.
+// emit: null, or 13 floats: position[3], velocity[3], colour[3], type
+// (0 square, 1 circle, 2 rectangle), radius, width, height.
 void* sfrg_create(const sf_params* p, const sf_boundary_params* b, const sf_solver_params* s,
-                  const sf_scene_init* in, int64_t capacity, int sort_multi) {
+                  const sf_scene_init* in, int64_t capacity, int sort_multi, const float* emit) {
     if (!p || !b || !s || !in || in->n <= 0 || capacity < in->n) return nullptr;
     cudaGetLastError();
     auto* r = new RefGpu();
@@ -104,8 +120,20 @@ void* sfrg_create(const sf_params* p, const sf_boundary_params* b, const sf_solv
     // the reference reads its globals at construction and at every UpdateSystem
     CUDA_SEEPAGEFLOW_PARAMS = P;
     CUDA_BOUNDARY_PARAMS = B;
-    CUDA_SPH_EMITTER_PARAMS.enable = false;
-    CUDA_SPH_EMITTER_PARAMS.run = false;
+    CUDA_SPH_EMITTER_PARAMS.enable = emit != nullptr;
+    CUDA_SPH_EMITTER_PARAMS.run = emit != nullptr;
+    if (emit) {
+        CUDA_SPH_EMITTER_PARAMS.emit_pos = f3(emit);
+        CUDA_SPH_EMITTER_PARAMS.emit_vel = f3(emit + 3);
+        CUDA_SPH_EMITTER_PARAMS.emit_col = f3(emit + 6);
+        CUDA_SPH_EMITTER_PARAMS.emit_type =
+            emit[9] == 1.f ? CudaSphEmitterType::CIRCLE
+                           : (emit[9] == 2.f ? CudaSphEmitterType::RECTANGLE : CudaSphEmitterType::SQUARE);
+        CUDA_SPH_EMITTER_PARAMS.emit_radius = emit[10];
+        CUDA_SPH_EMITTER_PARAMS.emit_width = emit[11];
+        CUDA_SPH_EMITTER_PARAMS.emit_height = emit[12];
+    }
+    r->E = CUDA_SPH_EMITTER_PARAMS;
 
     const size_t n = size_t(in->n);
     Vec_Float3 pos(n), col(n), cda(n);
@@ -141,7 +169,8 @@ void* sfrg_create(const sf_params* p, const sf_boundary_params* b, const sf_solv
                                                      s->speed_of_sound);
     else
         solver = std::make_shared<CudaSphSFSolver>(size_t(capacity));
-    CudaEmitterPtr emitter = std::make_shared<CudaEmitter>();
+    CudaEmitterPtr emitter = emit ? std::make_shared<CudaEmitter>(f3(emit), f3(emit + 3), true)
+                                  : std::make_shared<CudaEmitter>();
     // the system constructor moves from its arguments: hand it copies
     CudaSFParticlesPtr pArg = r->particles;
     CudaBoundaryParticlesPtr bArg = r->boundary;
@@ -164,6 +193,7 @@ float sfrg_update(void* h, float render_interval) {
     auto* r = static_cast<RefGpu*>(h);
     CUDA_SEEPAGEFLOW_PARAMS = r->P;
     CUDA_BOUNDARY_PARAMS = r->B;
+    CUDA_SPH_EMITTER_PARAMS = r->E;
     return r->system->UpdateSystem(render_interval);
 }
 
@@ -173,6 +203,7 @@ double sfrg_run(void* h, float render_interval, int64_t calls) {
     auto* r = static_cast<RefGpu*>(h);
     CUDA_SEEPAGEFLOW_PARAMS = r->P;
     CUDA_BOUNDARY_PARAMS = r->B;
+    CUDA_SPH_EMITTER_PARAMS = r->E;
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
@@ -194,8 +225,10 @@ int64_t sfrg_num_substeps(void* h) { return int64_t(static_cast<RefGpu*>(h)->sys
 
 int64_t sfrg_size(void* h) { return int64_t(static_cast<RefGpu*>(h)->particles->Size()); }
 
-// Field `field` (SF_FIELD_* / SF_BFIELD_*) in the reference's current order
-// as doubles (n x width); SF_FIELD_ID is the creation index.
+// Field `field` (SF_FIELD_* / SF_BFIELD_*, or kBFieldKey) in the reference's
+// current order as doubles (n x width); SF_FIELD_ID is the creation index
+// (emitted particles carry their radius there instead), SF_FIELD_KEY the
+// cell key of the last sort.
 int sfrg_get_field(void* h, int field, double* out, int64_t count) {
     auto* r = static_cast<RefGpu*>(h);
     const CudaSFParticlesPtr& P = r->particles;
@@ -242,6 +275,8 @@ int sfrg_get_field(void* h, int field, double* out, int64_t count) {
     case SF_FIELD_ADHESION: return put3(P->GetAdhesionForcePtr(), n);
     case SF_FIELD_AVG_ADHESION: return put3(P->GetAvgAdhesionForcePtr(), n);
     case SF_FIELD_CDA0ASAT: return put3(P->GetCdA0AsatPtr(), n);
+    case kFieldKey: return putS(r->searcher->GetGridIdxArrayPtr(), n);
+    case kBFieldKey: return putS(r->bsearcher->GetGridIdxArrayPtr(), r->nb);
     case SF_BFIELD_POS: return put3(r->boundary->GetPosPtr(), r->nb);
     case SF_BFIELD_LABEL: return putS(r->boundary->GetLabelPtr(), r->nb);
     case SF_BFIELD_VOLUME: return put1(r->boundary->GetVolumePtr(), r->nb);

@@ -298,9 +298,11 @@ struct Ref {
                 float desired = std::min(S.time_step_limit_scale * std::min(bySpeed, byForce), P.dt);
                 numSub = static_cast<size_t>(timeArg / desired);
             } else {
-                numSub = static_cast<size_t>(timeArg / P.dt);  // cuda_sph_sf_solver.cpp:24
+                numSub = static_cast<size_t>(timeArg / P.dt);  // cuda_sph_sf_solver.cpp:23
             }
-            dt = timeArg / static_cast<float>(numSub);
+            // WCSPH advects by renderInterval / N_sub (cuda_wcsph_sf_solver.cpp:168-172),
+            // plain SPH by params.dt (cuda_sph_sf_solver.cpp:141-146)
+            dt = P.solver_type == WCSPH_SOLVER ? timeArg / static_cast<float>(numSub) : P.dt;
         }
         // CudaSFParticles::Advect (cuda_sf_particles.cu:18-48) with AccDampingForSand
         // (cuda_sf_particles.cuh:19-40)

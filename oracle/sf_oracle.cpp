@@ -388,6 +388,34 @@ template <typename T> struct Sim {
         numSub = 1;
     }
 
+    // CudaSFParticles::AddSphParticles (cuda_sf_particles.cu:50-68): num water
+    // particles appended after the live ones with the given position, colour,
+    // velocity, mass and radius; refused when Size() + num >= MaxSize() (the
+    // caller passes the capacity). The reference leaves the new entries of the
+    // other arrays as they were; here they start at zero, which is what the
+    // next substep's passes overwrite or never read for water.
+    bool addSphParticles(const float* pos3, int64_t num, const float* c, const float* v, float m, float r,
+                         int64_t capacity) {
+        if (n + num >= capacity) return false;
+        const V3<T> zero = mk(T(0), T(0), T(0));
+        for (int64_t k = 0; k < num; ++k) {
+            label.push_back(0);
+            id.push_back(n + k);
+            key.push_back(0);
+            pos.push_back(f3(pos3 + 3 * k));
+            vel.push_back(f3(v));
+            col.push_back(f3(c));
+            mass.push_back(T(m));
+            radius.push_back(T(r));
+            for (auto* a : {&acc, &avgFlow, &avgDrag, &adhesion, &avgAdhesion, &cda0asat}) a->push_back(zero);
+            for (auto* a : {&density, &pressure, &voidage, &saturation, &maxSat, &amc, &amcp, &accScale,
+                            &pressureScale})
+                a->push_back(T(0));
+        }
+        n += num;
+        return true;
+    }
+
     // Stable counting sort by key: the permutation thrust::sort_by_key gives
     // for integer keys (SRCH:64-116).
     std::vector<int64_t> stableOrder(const std::vector<int64_t>& k, std::vector<int64_t>& start) const {
@@ -808,7 +836,7 @@ template <typename T> struct Sim {
 
     // ComputeSubTimeStepsByCFL (WCSPH.cu:35-58): the first maximum of |acc|
     // over all particles; N_sub = (size_t)(T / dt*). Plain SPH uses
-    // renderInterval / params.dt (SOLV.cpp:14-16).
+    // renderInterval / params.dt (SOLV.cpp:23).
     void cflPass(T renderInterval) {
         int64_t best = 0;
         T bestLen = n > 0 ? length(acc[0]) : T(0);
@@ -831,6 +859,13 @@ template <typename T> struct Sim {
         } else {
             numSub = int64_t(renderInterval / T(P.dt));
         }
+    }
+
+    // dt of the adaptive substep's Advect: WCSPH advects by renderInterval /
+    // N_sub (WCSPH.cpp:168-172), plain SPH by params.dt whatever N_sub rounds
+    // to (SOLV.cpp:23, 141-146).
+    T advectDt(T renderInterval) const {
+        return P.solver_type == SF_SOLVER_WCSPH ? renderInterval / T(numSub) : T(P.dt);
     }
 
     // CudaSphSFSolver::Advect (SOLV.cu:355-388) = CudaSFParticles::Advect
@@ -895,7 +930,7 @@ template <typename T> struct Sim {
             T dt = timeArg;
             if (adaptive) {
                 cflPass(timeArg);
-                dt = timeArg / T(numSub);
+                dt = advectDt(timeArg);
             }
             advectPass(dt);
             break;
@@ -920,7 +955,7 @@ template <typename T> struct Sim {
         T dt = timeArg;
         if (adaptive) {
             cflPass(timeArg);
-            dt = timeArg / T(numSub);
+            dt = advectDt(timeArg);
         }
         advectPass(dt);
     }
@@ -1124,6 +1159,16 @@ int sfo_frame_adaptive(void* hv, double render_interval, int64_t* n_calls) {
     });
     if (n_calls) *n_calls = calls;
     return SF_OK;
+}
+
+// AddSphParticles of num points (label 0); capacity plays MaxSize().
+// Returns SF_ERR_CAPACITY (nothing added) when Size() + num >= capacity.
+int sfo_add_sph_particles(void* hv, const float* pos3, int64_t num, const float* col, const float* vel, float mass,
+                          float radius, int64_t capacity) {
+    if (num < 0 || (num > 0 && !pos3) || !col || !vel) return SF_ERR_INVALID;
+    return static_cast<sfo::Handle*>(hv)->visit([&](auto& sim) {
+        return sim.addSphParticles(pos3, num, col, vel, mass, radius, capacity) ? int(SF_OK) : int(SF_ERR_CAPACITY);
+    });
 }
 
 int64_t sfo_num_substeps(void* hv) {

@@ -83,11 +83,30 @@ class Adam:
         return x - self.lr * mh / (np.sqrt(vh) + self.eps)
 
 
+# Seed scales of the adjoint (sf_set_adjoint_seed_scale): a scene whose
+# gradient overflowed FP32 in the reverse sweep is seeded 2^-40 smaller from
+# the next iteration on (powers of two change no rounding), down to 2^-100,
+# above which a seed of ~1e-3 stays clear of the subnormal range.
+SEED_STEP = 2.0 ** -40
+SEED_FLOOR = 2.0 ** -100
+
+
+def next_seed_scales(scales, finite):
+    """Seed scales for the next iteration: scenes without a finite gradient
+    this iteration get SEED_STEP times theirs (not below SEED_FLOOR)."""
+    out = np.asarray(scales, dtype=np.float64).copy()
+    bad = ~np.asarray(finite, dtype=bool)
+    out[bad] = np.maximum(out[bad] * SEED_STEP, SEED_FLOOR)
+    return out
+
+
 def calibrate(scenes, targets, theta0, dt, n_substeps, checkpoint_every, iterations, lr=0.02,
               relative_step=True, callback=None, autotune=True):
     """Adam on every scene's theta; returns the loss / theta history and the
     device milliseconds of each batched adjoint run. With relative_step the
-    update acts on log theta (steps relative to each parameter's size)."""
+    update acts on log theta (steps relative to each parameter's size). A
+    scene whose gradient is not finite keeps its theta that iteration and is
+    seeded smaller from then on (next_seed_scales)."""
     from .capi import Simulation
     sim = Simulation(scenes)
     if autotune:
@@ -95,11 +114,13 @@ def calibrate(scenes, targets, theta0, dt, n_substeps, checkpoint_every, iterati
     theta = np.array(theta0, dtype=np.float64).reshape(len(scenes), 3)
     target = np.concatenate([np.asarray(t, np.float32).reshape(-1, 3) for t in targets])
     opt = Adam(theta.shape, lr)
-    history = {"loss": [], "theta": [], "ms": []}
+    history = {"loss": [], "theta": [], "ms": [], "seed_scale": []}
+    scales = np.ones(len(scenes))
     for it in range(iterations):
         for s, sc in enumerate(scenes):
             reset_state(sim, s, sc)
             apply_theta(sim, s, sc, theta[s])
+            sim.set_adjoint_seed_scale(float(scales[s]), scene=s)
         t0 = time.perf_counter()
         res = sim.adjoint(dt, n_substeps, target, checkpoint_every=checkpoint_every, want_state_grads=False)
         wall = time.perf_counter() - t0
@@ -112,6 +133,8 @@ def calibrate(scenes, targets, theta0, dt, n_substeps, checkpoint_every, iterati
         bad = ~np.all(np.isfinite(g), axis=1)
         g[bad] = 0.0
         history.setdefault("nonfinite_gradients", []).append(int(bad.sum()))
+        history["seed_scale"].append(scales.tolist())
+        scales = next_seed_scales(scales, ~bad)
         history["loss"].append(res["loss"].astype(np.float64).tolist())
         history["theta"].append(theta.tolist())
         history["ms"].append({"forward": res["ms_forward"], "reverse": res["ms_reverse"], "wall": 1e3 * wall})

@@ -88,6 +88,7 @@ def load(path: str = LIB_PATH):
         "sf_autotune": (i32, [H, f32, P(i32), P(i32)]),
         "sf_last_error_string": (ctypes.c_char_p, [H]),
         "sf_adjoint_run": (i32, [H, f32, i64, i64, P(f32), P(f32), P(f32), P(f32), P(f32), P(f32)]),
+        "sf_set_adjoint_seed_scale": (i32, [H, i32, f32]),
         "sf_cell_sort_noalloc": (i32, [P(SfBoundaryParams), ctypes.c_void_p, i64, ctypes.c_void_p, ctypes.c_void_p,
                                        H]),
         "sf_export_bgeo": (i32, [H, i32, ctypes.c_char_p, ctypes.c_char_p]),
@@ -358,6 +359,11 @@ class Simulation:
                                             _fptr(loss), _fptr(gp), _fptr(gx), _fptr(gv), _fptr(ms)))
         return {"loss": loss, "grad_params": gp, "grad_pos0": gx, "grad_vel0": gv,
                 "ms_forward": float(ms[0]), "ms_reverse": float(ms[1])}
+
+    def set_adjoint_seed_scale(self, scale: float, scene: int = 0):
+        """sf_set_adjoint_seed_scale: the scene's adjoint cotangents are seeded
+        with scale x dL/dx and the returned gradients divided by it."""
+        self._check(self.lib.sf_set_adjoint_seed_scale(self.h, int(scene), float(scale)))
 
     def add_sph_particles(self, pos, col, vel, mass: float, radius: float, scene: int = 0):
         p = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)

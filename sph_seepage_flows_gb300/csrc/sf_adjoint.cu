@@ -340,7 +340,7 @@ __global__ void kAdjSeed(const SceneDev* __restrict__ scenes, const int* __restr
             const float3 d = xyz(p) - mk3(target[3 * id], target[3 * id + 1], target[3 * id + 2]);
             l = dot3(d, d);
             ns = 1.f;
-            g = 2.f * d;
+            g = (2.f * S.adj_seed_scale) * d;
         }
         adjX[id] = f4(g);
         adjV[id] = make_float4(0.f, 0.f, 0.f, 0.f);

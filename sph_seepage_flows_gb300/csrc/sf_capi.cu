@@ -128,6 +128,7 @@ SceneDev makeSceneDev(const sf_params& P, const sf_boundary_params& B, const sf_
     S.cfl_hm = h * P.sph_mass;
     S.cfl_mass = P.sph_mass;
     S.cfl_scale = Sp.time_step_limit_scale;
+    S.adj_seed_scale = 1.f;
     S.params_dt = P.dt;
     S.wcsph = S.tait;
     return S;
@@ -528,9 +529,10 @@ int queueStateCopy(sf_handle* h) {
 
 // Reads the state copies that have landed (waiting for copy slot `waitSlot`,
 // if >= 0) and grows the particle lists when a density pass found a list
-// full: the new capacity holds the largest count reported plus the usual
-// headroom (at most kMaxNbr). The substeps in between walked the stencil for
-// the particles concerned, which gives the same results more slowly.
+// more than 7/8 full: the new capacity holds the largest count reported plus
+// the usual headroom (at most kMaxNbr). Particles whose list overflowed in
+// the substeps in between walked the stencil, which gives the same results
+// more slowly.
 sf_status growListsIfFull(sf_handle* h, int waitSlot) {
     unsigned need = 0;
     for (int k = 0; k < 2; ++k) {
@@ -824,9 +826,20 @@ sf_status sf_set_params(sf_handle* h, int32_t scene, const sf_params* p) {
     S.b_off = old.b_off;
     S.nb = old.nb;
     S.shape_boundary = old.shape_boundary;
+    S.adj_seed_scale = old.adj_seed_scale;
     h->hScenes[scene] = S;
     return h->cuda(cudaMemcpyAsync(h->dScenes + scene, &S, sizeof(SceneDev), cudaMemcpyHostToDevice, h->stream),
                    "upload params");
+}
+
+sf_status sf_set_adjoint_seed_scale(sf_handle* h, int32_t scene, float scale) {
+    if (!h || scene < 0 || scene >= h->nScenes) return SF_ERR_INVALID;
+    if (!(scale > 0.f) || !std::isfinite(scale)) return h->fail(SF_ERR_INVALID, "seed scale must be finite and > 0");
+    SceneDev& S = h->hScenes[scene];
+    S.adj_seed_scale = scale;
+    return h->cuda(cudaMemcpyAsync(&h->dScenes[scene].adj_seed_scale, &S.adj_seed_scale, sizeof(float),
+                                   cudaMemcpyHostToDevice, h->stream),
+                   "upload seed scale");
 }
 
 sf_status sf_get_params(const sf_handle* h, int32_t scene, sf_params* p) {
@@ -1996,8 +2009,10 @@ sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t che
             for (int k = 0; k < 3; ++k) g[k] += paramPart[3 * size_t(b) + size_t(k)];
         const double inv = ns > 0.0 ? 1.0 / ns : 0.0;
         loss_out[s] = float(l * inv);
+        // the cotangents were seeded with adj_seed_scale x dL/dx: take it out
+        const double ginv = inv / double(S.adj_seed_scale);
         if (grad_params_out)
-            for (int k = 0; k < 3; ++k) grad_params_out[3 * s + k] = float(g[k] * inv);
+            for (int k = 0; k < 3; ++k) grad_params_out[3 * s + k] = float(g[k] * ginv);
         const int64_t n = h->n[s];
         for (int which = 0; which < 2; ++which) {
             float* out = which ? grad_vel0_out : grad_pos0_out;
@@ -2010,9 +2025,9 @@ sf_status sf_adjoint_run(sf_handle* h, float dt, int64_t n_substeps, int64_t che
                 h->cuda(cudaStreamSynchronize(h->stream), "gradient sync"))
                 return SF_ERR_CUDA;
             for (int64_t i = 0; i < n; ++i) {
-                out[3 * (off + i)] = float(double(buf[size_t(i)].x) * inv);
-                out[3 * (off + i) + 1] = float(double(buf[size_t(i)].y) * inv);
-                out[3 * (off + i) + 2] = float(double(buf[size_t(i)].z) * inv);
+                out[3 * (off + i)] = float(double(buf[size_t(i)].x) * ginv);
+                out[3 * (off + i) + 1] = float(double(buf[size_t(i)].y) * ginv);
+                out[3 * (off + i) + 2] = float(double(buf[size_t(i)].z) * ginv);
             }
         }
         off += n;

@@ -71,6 +71,8 @@ struct SceneDev {
     // CFL (cuda_wcsph_sf_solver.cu:35-58)
     float cfl_by_speed, cfl_hm, cfl_mass, cfl_scale, params_dt;
     int wcsph;
+    // factor on the adjoint's seed cotangents (sf_set_adjoint_seed_scale; 1 by default)
+    float adj_seed_scale;
 };
 
 // Per-scene device scalars written by the passes.
@@ -79,7 +81,7 @@ struct SceneState {
     int n;                   // live particle count
     long long n_sub;         // sub-step count of the last integrate
     float dt;                // dt of the last integrate
-    unsigned int list_need;  // largest neighbour count that found its list full (0: none)
+    unsigned int list_need;  // largest neighbour count above 7/8 of the list capacity (0: none)
 };
 
 // ---------------------------------------------------------------- float3 math

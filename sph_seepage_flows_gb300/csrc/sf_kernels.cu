@@ -149,6 +149,17 @@ __device__ __forceinline__ float listDensity(const SceneDev& S, const NbrListsW&
     return d;
 }
 
+// Records a neighbour count above 7/8 of the list capacity in the scene's
+// list_need (the largest such count of the warp, one atomic per warp); the
+// host reads it after the call and grows the lists to hold it with headroom,
+// so that a slowly compressing state grows its lists before any overflows.
+__device__ __forceinline__ void recordListNeed(const NbrListsW& L, unsigned int& need, int count) {
+    if (count <= L.cap - L.cap / 8) return;
+    const unsigned active = __activemask();
+    const unsigned m = __reduce_max_sync(active, unsigned(count));
+    if ((threadIdx.x & 31u) == unsigned(__ffs(active) - 1)) atomicMax(&need, m);
+}
+
 // Builds the neighbour lists (sand / water / boundary, each in stencil
 // order, plus the sand-sand contact list) and computes the density, fused
 // with ComputeSFPressureByTait_CUDA (cuda_wcsph_sf_solver_gpu.cuh:19-44) or
@@ -264,9 +275,10 @@ __global__ void __launch_bounds__(kSlotAlign, 6) kDensity(const SceneDev* __rest
     L.cnt[slot] = unsigned(min(cS, 0xFFFF)) | (unsigned(min(cW, 0xFFFF)) << 16);
     L.bcnt[slot] = bc;
     L.ccnt[slot] = cc;
-    // a full list asks the host to grow the capacity; until then the passes
-    // walk the stencil for this particle (same results, slower)
-    if (!listed) atomicMax(&state[sid].list_need, unsigned(cS + cW));
+    // a list more than 7/8 full asks the host to grow the capacity before it
+    // overflows; a full one walks the stencil until then (same results,
+    // slower)
+    recordListNeed(L, state[sid].list_need, cS + cW);
     float density, pressure = 0.f;
     if (!water) {
         density = S.rho1;
@@ -484,9 +496,10 @@ __global__ void __launch_bounds__(kSlotAlign) kDensityLanes(const SceneDev* __re
     L.cnt[slot] = unsigned(min(cS, 0xFFFF)) | (unsigned(min(cW, 0xFFFF)) << 16);
     L.bcnt[slot] = bc;
     L.ccnt[slot] = cc;
-    // a full list asks the host to grow the capacity; until then the passes
-    // walk the stencil for this particle (same results, slower)
-    if (!listed) atomicMax(&state[sid].list_need, unsigned(cS + cW));
+    // a list more than 7/8 full asks the host to grow the capacity before it
+    // overflows; a full one walks the stencil until then (same results,
+    // slower)
+    recordListNeed(L, state[sid].list_need, cS + cW);
     float pressure = 0.f;
     if (water) {
         if (S.tait) {
@@ -723,8 +736,11 @@ __global__ void kIntegrate(const SceneDev* __restrict__ scenes, const int* __res
     if (timeArgDev) timeArg = *timeArgDev;  // a graph-replayed step reads the time from the device
     float dt = timeArg;
     if (adaptive) {
+        // WCSPH advects by renderInterval / N_sub (cuda_wcsph_sf_solver.cpp:168-172); plain
+        // SPH by params.dt, whatever N_sub = renderInterval / params.dt rounds to
+        // (cuda_sph_sf_solver.cpp:23, 141-146)
         const long long ns = cflSubsteps(S, __uint_as_float(state[sid].amax_bits), timeArg);
-        dt = timeArg / float(ns);
+        dt = S.wcsph ? timeArg / float(ns) : S.params_dt;
         if (slot == S.slot_off) {
             state[sid].n_sub = ns;
             state[sid].dt = dt;

@@ -8,6 +8,7 @@ from sph_seepage_flows_gb300.params import SfBoundaryParams, SfParams, SfSolverP
 from sph_seepage_flows_gb300.scenes import Scene
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def load_golden(name):
@@ -37,6 +38,20 @@ def rel_err(a, b, scale=None, floor_frac=1e-3):
     scale = np.asarray(scale, np.float64)
     floor = floor_frac * (scale.max() if scale.size else 0.0) + 1e-30
     return float((d / np.maximum(scale, floor)).max()) if d.size else 0.0
+
+
+def rel_err_q(a, b, scale=None, q=0.999, floor_frac=1e-3):
+    """rel_err's per-particle errors at quantile q instead of the maximum."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    d = np.abs(a - b)
+    if d.ndim == 2:
+        d = np.linalg.norm(d, axis=1)
+    if scale is None:
+        scale = np.linalg.norm(b, axis=1) if b.ndim == 2 else np.abs(b)
+    scale = np.asarray(scale, np.float64)
+    floor = floor_frac * (scale.max() if scale.size else 0.0) + 1e-30
+    return float(np.quantile(d / np.maximum(scale, floor), q)) if d.size else 0.0
 
 
 def exact_fraction(a, b):
@@ -102,3 +117,34 @@ def compare_stages(sim, o32, time_arg, adaptive, tol, reps=1, stages=None, repor
                     assert frac == 1.0, (rep, st, name, frac, err)
             for name in CARRIED:
                 o32.set_field(name, sim.field(name))
+
+
+def build_facade_program(tmp_path, name):
+    """Compiles tests/cpp/<name>.cpp against the facade and libsf_gb300.so."""
+    import subprocess
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    exe = str(tmp_path / name)
+    pkg = os.path.join(ROOT, "sph_seepage_flows_gb300")
+    cmd = ["g++", "-std=c++17", "-O2", f'-DDB_PBR_PATH="{tmp_path}/"', "-I", os.path.join(ROOT, "include"),
+           "-I", f"{cuda}/include",
+           os.path.join(ROOT, "tests", "cpp", name + ".cpp"), "-o", exe, "-L", pkg, "-l:libsf_gb300.so",
+           f"-Wl,-rpath,{pkg}", "-L", f"{cuda}/lib64", "-lcudart"]
+    subprocess.run(cmd, check=True)
+    return exe
+
+
+def facade_scene(init_pos):
+    """The scene the facade programs (tests/cpp/facade_scene.hpp) build, with
+    their (seeded) initial positions."""
+    from sph_seepage_flows_gb300 import scenes
+    from sph_seepage_flows_gb300.params import SF_LABEL_SAND, SF_LABEL_WATER
+    ns, nw = 8 * 6 * 8, 7 * 10 * 8
+    sc = scenes.block_scene("facade", (0.4, 0.4, 0.4), (8, 6, 8), (7, 10, 8), 0.02, 0, jitter_frac=0.0,
+                            sand_origin=(0.22, 0.02, 0.08), water_origin=(0.06, 0.02, 0.08))
+    assert sc.n == ns + nw
+    sc.pos = init_pos.astype(np.float32)
+    sc.col = sc.col.copy()
+    sc.col[sc.label == SF_LABEL_WATER] = np.array([0.5, 0.8, 1.0], np.float32)
+    sc.cda0asat = np.zeros((sc.n, 3), np.float32)
+    sc.cda0asat[sc.label == SF_LABEL_SAND] = [0.5, 0.0, 0.8]
+    return sc

@@ -43,3 +43,11 @@ def test_calibration_scene_sizes():
     scs = scenes.calibration_scenes()
     n = np.array([s.n for s in scs])
     assert len(scs) == 32 and n.min() >= 9_000 and n.max() <= 55_000
+
+
+def test_seed_scales_shrink_only_where_the_gradient_overflowed():
+    s = calibrate.next_seed_scales([1.0, 1.0, 2.0 ** -40, 2.0 ** -90], [True, False, False, False])
+    assert s[0] == 1.0
+    assert s[1] == 2.0 ** -40 and s[2] == 2.0 ** -80
+    assert s[3] == calibrate.SEED_FLOOR  # never below the floor
+    assert all(np.log2(v).is_integer() for v in s)  # powers of two: no rounding changes

@@ -180,3 +180,27 @@ def test_long_horizon_gradients_stay_finite(cuda_lib):
         for key in ("loss", "grad_params", "grad_pos0", "grad_vel0"):
             assert np.all(np.isfinite(r[key])), key
         calibrate.reset_state(sim, 0, sc)
+
+
+def test_seed_scale_changes_no_gradient_bit(cuda_lib):
+    """sf_set_adjoint_seed_scale with a power of two: every cotangent of the
+    reverse sweep is scaled exactly, so after the scale is divided out the
+    gradients equal the unscaled run's bit for bit; sf_set_params keeps it."""
+    sc = probe_scene(11, 0.4)
+    target = probe_target(sc)
+    outs = []
+    for scale in (1.0, 2.0 ** -20, 2.0 ** 12):
+        sim = sim_of(sc)
+        sim.set_adjoint_seed_scale(scale)
+        sim.set_params(sc.params)
+        outs.append(sim.adjoint(DT, 8, target, checkpoint_every=4))
+        sim.close()
+    for r in outs[1:]:
+        for key in ("loss", "grad_params", "grad_pos0", "grad_vel0"):
+            assert np.array_equal(r[key], outs[0][key]), key
+    from sph_seepage_flows_gb300.capi import SfError
+    sim = sim_of(sc)
+    for bad in (0.0, -1.0, float("inf"), float("nan")):
+        with pytest.raises(SfError):
+            sim.set_adjoint_seed_scale(bad)
+    sim.close()

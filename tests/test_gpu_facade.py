@@ -3,49 +3,19 @@ the reference app (tests/cpp/facade_main.cpp) compiles against the facade and
 libsf_gb300.so, runs one adaptive frame, and ends in the same state as the
 Python binding of the C ABI run from the same initial state."""
 
-import os
 import subprocess
 
 import numpy as np
 import pytest
 
-from sph_seepage_flows_gb300 import scenes
-from sph_seepage_flows_gb300.params import SF_LABEL_SAND, SF_LABEL_WATER
+from helpers import build_facade_program, facade_scene
 
 pytestmark = pytest.mark.gpu
-
-ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-
-
-def build_program(tmp_path):
-    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
-    exe = str(tmp_path / "facade_main")
-    pkg = os.path.join(ROOT, "sph_seepage_flows_gb300")
-    cmd = ["g++", "-std=c++17", "-O2", f'-DDB_PBR_PATH="{tmp_path}/"', "-I", os.path.join(ROOT, "include"),
-           "-I", f"{cuda}/include",
-           os.path.join(ROOT, "tests", "cpp", "facade_main.cpp"), "-o", exe, "-L", pkg, "-l:libsf_gb300.so",
-           f"-Wl,-rpath,{pkg}", "-L", f"{cuda}/lib64", "-lcudart"]
-    subprocess.run(cmd, check=True)
-    return exe
-
-
-def facade_scene(init_pos):
-    """The scene facade_main.cpp builds, with its (seeded) initial positions."""
-    ns, nw = 8 * 6 * 8, 7 * 10 * 8
-    sc = scenes.block_scene("facade", (0.4, 0.4, 0.4), (8, 6, 8), (7, 10, 8), 0.02, 0, jitter_frac=0.0,
-                            sand_origin=(0.22, 0.02, 0.08), water_origin=(0.06, 0.02, 0.08))
-    assert sc.n == ns + nw
-    sc.pos = init_pos.astype(np.float32)
-    sc.col = sc.col.copy()
-    sc.col[sc.label == SF_LABEL_WATER] = np.array([0.5, 0.8, 1.0], np.float32)
-    sc.cda0asat = np.zeros((sc.n, 3), np.float32)
-    sc.cda0asat[sc.label == SF_LABEL_SAND] = [0.5, 0.0, 0.8]
-    return sc
 
 
 def test_facade_program_matches_c_abi(cuda_lib, tmp_path):
     from sph_seepage_flows_gb300.capi import Simulation
-    exe = build_program(tmp_path)
+    exe = build_facade_program(tmp_path, "facade_main")
     dump = str(tmp_path / "dump.bin")
     export = tmp_path / "bgeo" / "out"   # the reader's DB_PBR_PATH "bgeo/out"
     out = subprocess.run([exe, dump, "1", str(export)], capture_output=True, text=True, timeout=300)

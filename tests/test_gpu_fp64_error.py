@@ -25,7 +25,7 @@ through the oracle's particle ids (summation order is immaterial in FP64).
 import numpy as np
 import pytest
 
-from helpers import CARRIED, STAGE_OUTPUTS, rel_err
+from helpers import CARRIED, STAGE_OUTPUTS, rel_err, rel_err_q
 from sph_seepage_flows_gb300 import scenes
 from sph_seepage_flows_gb300.params import STAGES, reference_dt
 from sph_seepage_flows_gb300.scenes import Scene
@@ -41,20 +41,6 @@ def sorted_scene(sim, sc):
     return Scene(name=sc.name + "_sorted", params=sc.params, bparams=sc.bparams, sparams=sc.sparams,
                  pos=f["pos"], vel=f["vel"], col=f["col"], label=f["label"], mass=f["mass"], radius=f["radius"],
                  cda0asat=f["cda0asat"], amcamcp=f["amcamcp"], bpos=sc.bpos, blabel=sc.blabel)
-
-
-def rel_err_q(a, b, scale=None, q=0.999, floor_frac=1e-3):
-    """rel_err's per-particle errors at quantile q instead of the maximum."""
-    a = np.asarray(a, np.float64)
-    b = np.asarray(b, np.float64)
-    d = np.abs(a - b)
-    if d.ndim == 2:
-        d = np.linalg.norm(d, axis=1)
-    if scale is None:
-        scale = np.linalg.norm(b, axis=1) if b.ndim == 2 else np.abs(b)
-    scale = np.asarray(scale, np.float64)
-    floor = floor_frac * (scale.max() if scale.size else 0.0) + 1e-30
-    return float(np.quantile(d / np.maximum(scale, floor), q)) if d.size else 0.0
 
 
 def fp64_errors(oracle_mod, sc, time_arg, adaptive):

@@ -1,9 +1,10 @@
 """Neighbour-list growth (sf_get_list_capacity). A density pass that finds a
-particle's list full records the particle's neighbour count; until the host
-has read that record the particle's passes walk the stencil, and then the
-handle re-allocates its lists. Lists and stencil walks visit the same
-neighbours in the same order, so a handle whose lists grow computes the same
-states, bit for bit, as one created with lists large enough from the start."""
+particle's list more than 7/8 full records the particle's neighbour count;
+the host reads that record after the call and re-allocates the lists (a
+particle whose list overflowed meanwhile walks the stencil). Lists and
+stencil walks visit the same neighbours in the same order, so a handle whose
+lists grow computes the same states, bit for bit, as one created with lists
+large enough from the start."""
 
 import numpy as np
 import pytest
