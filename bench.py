@@ -62,8 +62,8 @@ BYTES_PER_SUBSTEP = sum(STAGE_BYTES.values())  # 753
 # workload, from one ncu capture, tagged with the digest of the kernel sources
 # it was taken on (csrc_digest()). When the sources have changed since, the
 # figure no longer describes the running kernels and is reported as null.
-NCU_TRAFFIC_DIGEST = ""
-NCU_TRAFFIC = {}
+NCU_TRAFFIC_DIGEST = "99b51a29fa5a"
+NCU_TRAFFIC = {"density": 283.3e6}
 
 
 def csrc_digest() -> str:

@@ -224,25 +224,30 @@ public:
                     const Vec_Float& radius)
         : CudaSFParticles(p.size(), p, col, label, mass, radius) {}
 
-    // CudaSFParticles getters (cuda_sf_particles.cuh:170-190): device copies in sorted order.
-    float3* GetPosPtr() const { return static_cast<float3*>(field(SF_FIELD_POS, 12)); }
-    float3* GetVelPtr() const { return static_cast<float3*>(field(SF_FIELD_VEL, 12)); }
-    float3* GetAccPtr() const { return static_cast<float3*>(field(SF_FIELD_ACC, 12)); }
-    float3* GetColPtr() const { return static_cast<float3*>(field(SF_FIELD_COL, 12)); }
-    float* GetRadiusPtr() const { return static_cast<float*>(field(SF_FIELD_RADIUS, 4)); }
-    float* GetMassPtr() const { return static_cast<float*>(field(SF_FIELD_MASS, 4)); }
-    float* GetDensityPtr() const { return static_cast<float*>(field(SF_FIELD_DENSITY, 4)); }
-    float* GetPressurePtr() const { return static_cast<float*>(field(SF_FIELD_PRESSURE, 4)); }
-    float* GetVoidagePtr() const { return static_cast<float*>(field(SF_FIELD_VOIDAGE, 4)); }
-    float* GetSaturationPtr() const { return static_cast<float*>(field(SF_FIELD_SATURATION, 4)); }
-    float* GetMaxSaturationPtr() const { return static_cast<float*>(field(SF_FIELD_MAX_SATURATION, 4)); }
-    float3* GetAvgFlowVelPtr() const { return static_cast<float3*>(field(SF_FIELD_AVG_FLOW, 12)); }
-    float3* GetAvgDragForcePtr() const { return static_cast<float3*>(field(SF_FIELD_AVG_DRAG, 12)); }
-    float3* GetAdhesionForcePtr() const { return static_cast<float3*>(field(SF_FIELD_ADHESION, 12)); }
-    float3* GetAvgAdhesionForcePtr() const { return static_cast<float3*>(field(SF_FIELD_AVG_ADHESION, 12)); }
-    float3* GetCdA0AsatPtr() const { return static_cast<float3*>(field(SF_FIELD_CDA0ASAT, 12)); }
-    float2* GetAmcAmcpPtr() const { return static_cast<float2*>(field(SF_FIELD_AMCAMCP, 8)); }
-    size_t* GetLabelPtr() const;
+    // CudaSFParticles getters (cuda_sf_particles.cuh:170-190): device copies in
+    // sorted order, refreshed by each call. The reference returns writable
+    // pointers into its own arrays; these are copies, so they are const: code
+    // that writes through a getter (which would change nothing here) fails to
+    // compile instead of silently doing nothing. Change a field with
+    // sf_set_field on Handle().
+    const float3* GetPosPtr() const { return static_cast<const float3*>(field(SF_FIELD_POS, 12)); }
+    const float3* GetVelPtr() const { return static_cast<const float3*>(field(SF_FIELD_VEL, 12)); }
+    const float3* GetAccPtr() const { return static_cast<const float3*>(field(SF_FIELD_ACC, 12)); }
+    const float3* GetColPtr() const { return static_cast<const float3*>(field(SF_FIELD_COL, 12)); }
+    const float* GetRadiusPtr() const { return static_cast<const float*>(field(SF_FIELD_RADIUS, 4)); }
+    const float* GetMassPtr() const { return static_cast<const float*>(field(SF_FIELD_MASS, 4)); }
+    const float* GetDensityPtr() const { return static_cast<const float*>(field(SF_FIELD_DENSITY, 4)); }
+    const float* GetPressurePtr() const { return static_cast<const float*>(field(SF_FIELD_PRESSURE, 4)); }
+    const float* GetVoidagePtr() const { return static_cast<const float*>(field(SF_FIELD_VOIDAGE, 4)); }
+    const float* GetSaturationPtr() const { return static_cast<const float*>(field(SF_FIELD_SATURATION, 4)); }
+    const float* GetMaxSaturationPtr() const { return static_cast<const float*>(field(SF_FIELD_MAX_SATURATION, 4)); }
+    const float3* GetAvgFlowVelPtr() const { return static_cast<const float3*>(field(SF_FIELD_AVG_FLOW, 12)); }
+    const float3* GetAvgDragForcePtr() const { return static_cast<const float3*>(field(SF_FIELD_AVG_DRAG, 12)); }
+    const float3* GetAdhesionForcePtr() const { return static_cast<const float3*>(field(SF_FIELD_ADHESION, 12)); }
+    const float3* GetAvgAdhesionForcePtr() const { return static_cast<const float3*>(field(SF_FIELD_AVG_ADHESION, 12)); }
+    const float3* GetCdA0AsatPtr() const { return static_cast<const float3*>(field(SF_FIELD_CDA0ASAT, 12)); }
+    const float2* GetAmcAmcpPtr() const { return static_cast<const float2*>(field(SF_FIELD_AMCAMCP, 8)); }
+    const size_t* GetLabelPtr() const;
 
     // CudaSFParticles::AddSphParticles (cuda_sf_particles.cu:50-68)
     void AddSphParticles(Vec_Float3 pos, float3 col, float3 vel, float mass, float radius);
@@ -298,7 +303,7 @@ public:
     // particles (boundary particles for the boundary searcher) and the count
     // at entry G. A copy of the table of the last sort, refreshed by each
     // call; nullptr before the searcher's system exists.
-    size_t* GetCellStartPtr() const;
+    const size_t* GetCellStartPtr() const;
 
 protected:
     static float3 f3div(float3 a, float s) { return make_float3(a.x / s, a.y / s, a.z / s); }
@@ -699,7 +704,7 @@ inline size_t CudaParticles::Size() const {
     return size_t(n);
 }
 
-inline size_t* CudaGNBaseSearcher::GetCellStartPtr() const {
+inline const size_t* CudaGNBaseSearcher::GetCellStartPtr() const {
     if (!mSystem || !mSystem->Handle()) return nullptr;
     int32_t g[3];
     int64_t cells = 0;
@@ -723,7 +728,7 @@ inline void* CudaSFParticles::field(int id, size_t elemBytes) const {
     return d;
 }
 
-inline size_t* CudaSFParticles::GetLabelPtr() const {
+inline const size_t* CudaSFParticles::GetLabelPtr() const {
     if (!mSystem || !mSystem->Handle()) return nullptr;
     const size_t n = Size();
     std::vector<int32_t> l(n);

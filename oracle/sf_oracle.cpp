@@ -41,69 +41,110 @@
 
 namespace sfo {
 
-// Forward-mode dual number: an FP64 value and one tangent. Sim<Dual1> runs
-// the FP64 restatement while carrying the derivative of every quantity
-// along one direction (initial positions / velocities or one parameter), the
-// exact pathwise directional derivative that a reverse-mode gradient must
-// reproduce. Comparisons and branches use the value.
-struct Dual1 {
-    double v = 0.0, d = 0.0;
-    Dual1() = default;
-    Dual1(double x) : v(x), d(0.0) {}  // NOLINT: constants convert implicitly
-    Dual1(double x, double t) : v(x), d(t) {}
-    explicit operator double() const { return v; }
+// Forward-mode dual number: a value and one FP64 tangent. Sim<Dual1> (FP64
+// values) runs the FP64 restatement while carrying the derivative of every
+// quantity along one direction (initial positions / velocities or one
+// parameter), the exact pathwise directional derivative that a reverse-mode
+// gradient must reproduce. Sim<DualF> does the same on the FP32 trajectory:
+// its values are formed with the FP32 restatement's float operations in the
+// same order, so they equal Sim<float>'s bit for bit. Comparisons and
+// branches use the value.
+template <typename V> struct DualT {
+    V v = V(0);
+    double d = 0.0;
+    DualT() = default;
+    DualT(double x) : v(V(x)), d(0.0) {}  // NOLINT: constants convert implicitly
+    DualT(double x, double t) : v(V(x)), d(t) {}
+    explicit operator double() const { return double(v); }
     explicit operator float() const { return float(v); }
     explicit operator int() const { return int(v); }
     explicit operator long() const { return long(v); }
     explicit operator long long() const { return (long long)(v); }
-    Dual1& operator+=(Dual1 b) { v += b.v; d += b.d; return *this; }
-    Dual1& operator-=(Dual1 b) { v -= b.v; d -= b.d; return *this; }
-    Dual1& operator*=(Dual1 b) { d = d * b.v + v * b.d; v *= b.v; return *this; }
-    Dual1& operator/=(Dual1 b) { const double q = v / b.v; d = (d - q * b.d) / b.v; v = q; return *this; }
+    DualT& operator+=(DualT b) { v += b.v; d += b.d; return *this; }
+    DualT& operator-=(DualT b) { v -= b.v; d -= b.d; return *this; }
+    DualT& operator*=(DualT b) { d = d * double(b.v) + double(v) * b.d; v *= b.v; return *this; }
+    DualT& operator/=(DualT b) {
+        const V q = v / b.v;
+        d = (d - double(q) * b.d) / double(b.v);
+        v = q;
+        return *this;
+    }
 };
-inline Dual1 operator+(Dual1 a, Dual1 b) { return Dual1(a.v + b.v, a.d + b.d); }
-inline Dual1 operator-(Dual1 a, Dual1 b) { return Dual1(a.v - b.v, a.d - b.d); }
-inline Dual1 operator-(Dual1 a) { return Dual1(-a.v, -a.d); }
-inline Dual1 operator*(Dual1 a, Dual1 b) { return Dual1(a.v * b.v, a.d * b.v + a.v * b.d); }
-inline Dual1 operator/(Dual1 a, Dual1 b) { const double q = a.v / b.v; return Dual1(q, (a.d - q * b.d) / b.v); }
-inline bool operator<(Dual1 a, Dual1 b) { return a.v < b.v; }
-inline bool operator>(Dual1 a, Dual1 b) { return a.v > b.v; }
-inline bool operator<=(Dual1 a, Dual1 b) { return a.v <= b.v; }
-inline bool operator>=(Dual1 a, Dual1 b) { return a.v >= b.v; }
-inline bool operator==(Dual1 a, Dual1 b) { return a.v == b.v; }
-inline bool operator!=(Dual1 a, Dual1 b) { return a.v != b.v; }
+using Dual1 = DualT<double>;
+using DualF = DualT<float>;
+template <typename V> inline DualT<V> mkDual(V v, double d) {
+    DualT<V> r;
+    r.v = v;
+    r.d = d;
+    return r;
+}
+template <typename V> inline DualT<V> operator+(DualT<V> a, DualT<V> b) { return mkDual(V(a.v + b.v), a.d + b.d); }
+template <typename V> inline DualT<V> operator-(DualT<V> a, DualT<V> b) { return mkDual(V(a.v - b.v), a.d - b.d); }
+template <typename V> inline DualT<V> operator-(DualT<V> a) { return mkDual(V(-a.v), -a.d); }
+template <typename V> inline DualT<V> operator*(DualT<V> a, DualT<V> b) {
+    return mkDual(V(a.v * b.v), a.d * double(b.v) + double(a.v) * b.d);
+}
+template <typename V> inline DualT<V> operator/(DualT<V> a, DualT<V> b) {
+    const V q = a.v / b.v;
+    return mkDual(q, (a.d - double(q) * b.d) / double(b.v));
+}
+template <typename V> inline bool operator<(DualT<V> a, DualT<V> b) { return a.v < b.v; }
+template <typename V> inline bool operator>(DualT<V> a, DualT<V> b) { return a.v > b.v; }
+template <typename V> inline bool operator<=(DualT<V> a, DualT<V> b) { return a.v <= b.v; }
+template <typename V> inline bool operator>=(DualT<V> a, DualT<V> b) { return a.v >= b.v; }
+template <typename V> inline bool operator==(DualT<V> a, DualT<V> b) { return a.v == b.v; }
+template <typename V> inline bool operator!=(DualT<V> a, DualT<V> b) { return a.v != b.v; }
+// mixed with plain numbers (the value type's constants)
+template <typename V> inline DualT<V> operator+(DualT<V> a, double b) { return a + DualT<V>(b); }
+template <typename V> inline DualT<V> operator+(double a, DualT<V> b) { return DualT<V>(a) + b; }
+template <typename V> inline DualT<V> operator-(DualT<V> a, double b) { return a - DualT<V>(b); }
+template <typename V> inline DualT<V> operator-(double a, DualT<V> b) { return DualT<V>(a) - b; }
+template <typename V> inline DualT<V> operator*(DualT<V> a, double b) { return a * DualT<V>(b); }
+template <typename V> inline DualT<V> operator*(double a, DualT<V> b) { return DualT<V>(a) * b; }
+template <typename V> inline DualT<V> operator/(DualT<V> a, double b) { return a / DualT<V>(b); }
+template <typename V> inline DualT<V> operator/(double a, DualT<V> b) { return DualT<V>(a) / b; }
+template <typename V> inline bool operator<(DualT<V> a, double b) { return a.v < V(b); }
+template <typename V> inline bool operator>(DualT<V> a, double b) { return a.v > V(b); }
+template <typename V> inline bool operator<(double a, DualT<V> b) { return V(a) < b.v; }
+template <typename V> inline bool operator>(double a, DualT<V> b) { return V(a) > b.v; }
 
 // Math functions of the restatement: the std functions for float / double,
-// their derivatives for Dual1.
+// their derivatives for the dual numbers (values by the value type's std
+// function, as the plain restatement of that precision forms them).
 inline float tsqrt(float x) { return std::sqrt(x); }
 inline double tsqrt(double x) { return std::sqrt(x); }
-inline Dual1 tsqrt(Dual1 a) {
-    const double r = std::sqrt(a.v);
-    return Dual1(r, r > 0.0 ? a.d / (2.0 * r) : 0.0);
+template <typename V> inline DualT<V> tsqrt(DualT<V> a) {
+    const V r = std::sqrt(a.v);
+    return mkDual(r, r > V(0) ? a.d / (2.0 * double(r)) : 0.0);
 }
 inline float tpow(float a, float b) { return std::pow(a, b); }
 inline double tpow(double a, double b) { return std::pow(a, b); }
-inline Dual1 tpow(Dual1 a, Dual1 b) {
-    const double r = std::pow(a.v, b.v);
-    double d = a.v != 0.0 ? b.v * std::pow(a.v, b.v - 1.0) * a.d : 0.0;
-    if (b.d != 0.0 && a.v > 0.0) d += std::log(a.v) * r * b.d;
-    return Dual1(r, d);
+template <typename V> inline DualT<V> tpow(DualT<V> a, DualT<V> b) {
+    const V r = std::pow(a.v, b.v);
+    const double av = double(a.v), bv = double(b.v);
+    double d = av != 0.0 ? bv * std::pow(av, bv - 1.0) * a.d : 0.0;
+    if (b.d != 0.0 && av > 0.0) d += std::log(av) * double(r) * b.d;
+    return mkDual(r, d);
 }
 inline float tfmax(float a, float b) { return std::fmax(a, b); }
 inline double tfmax(double a, double b) { return std::fmax(a, b); }
-inline Dual1 tfmax(Dual1 a, Dual1 b) { return (a.v > b.v || b.v != b.v) ? a : b; }
+template <typename V> inline DualT<V> tfmax(DualT<V> a, DualT<V> b) { return (a.v > b.v || b.v != b.v) ? a : b; }
 inline float tfmin(float a, float b) { return std::fmin(a, b); }
 inline double tfmin(double a, double b) { return std::fmin(a, b); }
-inline Dual1 tfmin(Dual1 a, Dual1 b) { return (a.v < b.v || b.v != b.v) ? a : b; }
+template <typename V> inline DualT<V> tfmin(DualT<V> a, DualT<V> b) { return (a.v < b.v || b.v != b.v) ? a : b; }
 inline float tfabs(float x) { return std::fabs(x); }
 inline double tfabs(double x) { return std::fabs(x); }
-inline Dual1 tfabs(Dual1 a) { return a.v < 0.0 ? -a : a; }
+template <typename V> inline DualT<V> tfabs(DualT<V> a) { return a.v < V(0) ? -a : a; }
 inline float tcos(float x) { return std::cos(x); }
 inline double tcos(double x) { return std::cos(x); }
-inline Dual1 tcos(Dual1 a) { return Dual1(std::cos(a.v), -std::sin(a.v) * a.d); }
+template <typename V> inline DualT<V> tcos(DualT<V> a) {
+    return mkDual(V(std::cos(a.v)), -std::sin(double(a.v)) * a.d);
+}
 inline float tsin(float x) { return std::sin(x); }
 inline double tsin(double x) { return std::sin(x); }
-inline Dual1 tsin(Dual1 a) { return Dual1(std::sin(a.v), std::cos(a.v) * a.d); }
+template <typename V> inline DualT<V> tsin(DualT<V> a) {
+    return mkDual(V(std::sin(a.v)), std::cos(double(a.v)) * a.d);
+}
 
 // A parameter value, carrying the tangent t when T is Dual1.
 template <typename T> inline T seeded(float v, double t) {
@@ -111,6 +152,7 @@ template <typename T> inline T seeded(float v, double t) {
     return T(v);
 }
 template <> inline Dual1 seeded<Dual1>(float v, double t) { return Dual1(double(v), t); }
+template <> inline DualF seeded<DualF>(float v, double t) { return DualF(double(v), t); }
 
 // KIRI_EPSILON and KIRI_PI (seepage_flows_cuda/include/kiri_pbs_cuda/kiri_pbs_pch.cuh:52-54).
 template <typename T> constexpr T kEps() { return T(1e-6f); }
@@ -962,21 +1004,31 @@ template <typename T> struct Sim {
 };
 
 struct Handle {
-    int precision;  // 32, 64, or 65 = FP64 with one forward-mode tangent
+    // 32, 64, 65 = FP64 with one forward-mode tangent, 66 = the FP32
+    // trajectory with one FP64 forward-mode tangent
+    int precision;
     Sim<float> f;
     Sim<double> d;
     Sim<Dual1> j;
+    Sim<DualF> jf;
     template <typename F> auto visit(F&& fn) {
+        if (precision == 66) return fn(jf);
         if (precision == 65) return fn(j);
         if (precision == 64) return fn(d);
         return fn(f);
     }
+    // the forward-mode handles only
+    template <typename F> int visitDual(F&& fn) {
+        if (precision == 66) return fn(jf);
+        if (precision == 65) return fn(j);
+        return SF_ERR_INVALID;
+    }
 };
 
-// Tangents (Sim<Dual1>) of positions or velocities, in the current internal order.
-inline int tangentField(Sim<Dual1>& s, int field, double* get, const double* set, int64_t count) {
+// Tangents (Sim<Dual1> / Sim<DualF>) of positions or velocities, in the current internal order.
+template <typename D> inline int tangentField(Sim<D>& s, int field, double* get, const double* set, int64_t count) {
     if (count != s.n || (field != SF_FIELD_POS && field != SF_FIELD_VEL)) return SF_ERR_INVALID;
-    std::vector<V3<Dual1>>& a = field == SF_FIELD_POS ? s.pos : s.vel;
+    std::vector<V3<D>>& a = field == SF_FIELD_POS ? s.pos : s.vel;
     for (int64_t i = 0; i < s.n; ++i) {
         if (set) {
             a[i].x.d = set[3 * i];
@@ -1090,7 +1142,7 @@ extern "C" {
 void* sfo_create(int precision, const sf_params* p, const sf_boundary_params* b, const sf_solver_params* s,
                  const sf_scene_init* in, int sort_multi) {
     auto* h = new sfo::Handle();
-    h->precision = (precision == 64 || precision == 65) ? precision : 32;
+    h->precision = (precision == 64 || precision == 65 || precision == 66) ? precision : 32;
     h->visit([&](auto& sim) {
         sim.init(p, b, s, in, sort_multi);
         return 0;
@@ -1183,25 +1235,25 @@ double sfo_max_acc(void* hv) {
 // (3 doubles per particle, current internal order; before the first sort
 // that is the creation order) and the parameter to differentiate by.
 int sfo_set_tangent(void* hv, int field, const double* src, int64_t count) {
-    auto* h = static_cast<sfo::Handle*>(hv);
-    if (h->precision != 65) return SF_ERR_INVALID;
-    return sfo::tangentField(h->j, field, nullptr, src, count);
+    return static_cast<sfo::Handle*>(hv)->visitDual(
+        [&](auto& s) { return sfo::tangentField(s, field, nullptr, src, count); });
 }
 
 int sfo_get_tangent(void* hv, int field, double* dst, int64_t count) {
-    auto* h = static_cast<sfo::Handle*>(hv);
-    if (h->precision != 65) return SF_ERR_INVALID;
-    return sfo::tangentField(h->j, field, dst, nullptr, count);
+    return static_cast<sfo::Handle*>(hv)->visitDual(
+        [&](auto& s) { return sfo::tangentField(s, field, dst, nullptr, count); });
 }
 
 // which: 0 none, 1 tan friction angle, 2 capillary scale, 3 permeability scale.
 // The permeability tangent also seeds the per-particle cd of sand (MULTI scenes).
 int sfo_seed_param(void* hv, int which) {
-    auto* h = static_cast<sfo::Handle*>(hv);
-    if (h->precision != 65 || which < 0 || which > 3) return SF_ERR_INVALID;
-    h->j.seedParam = which;
-    for (int64_t i = 0; i < h->j.n; ++i) h->j.cda0asat[i].x.d = (which == 3 && h->j.label[i] == 1) ? h->j.cda0asat[i].x.v : 0.0;
-    return SF_OK;
+    if (which < 0 || which > 3) return SF_ERR_INVALID;
+    return static_cast<sfo::Handle*>(hv)->visitDual([&](auto& s) {
+        s.seedParam = which;
+        for (int64_t i = 0; i < s.n; ++i)
+            s.cda0asat[i].x.d = (which == 3 && s.label[i] == 1) ? double(s.cda0asat[i].x.v) : 0.0;
+        return int(SF_OK);
+    });
 }
 
 // Largest distance at which a pair term can be non-zero for these params.

@@ -65,7 +65,7 @@ int main(int argc, char** argv) {
     if (sf_get_field(system.Handle(), 0, SF_FIELD_POS, SF_ORDER_ID, out.data(), int64_t(n), 0) != SF_OK) return 5;
     std::fwrite(out.data(), sizeof(float), out.size(), f);
     std::fclose(f);
-    float3* dpos = particles->GetPosPtr();
+    const float3* dpos = particles->GetPosPtr();
     // the searchers' cell tables (GetCellStartPtr): G + 1 monotone entries
     // ending with the particle / boundary count
     for (int which = 0; which < 2; ++which) {
@@ -73,7 +73,7 @@ int main(int argc, char** argv) {
                                              : static_cast<const CudaGNBaseSearcher&>(*searcher);
         const int3 g = se.GetGridSize();
         std::vector<size_t> t(size_t(g.x) * g.y * g.z + 1);
-        size_t* d = se.GetCellStartPtr();
+        const size_t* d = se.GetCellStartPtr();
         if (!d || cudaMemcpy(t.data(), d, t.size() * sizeof(size_t), cudaMemcpyDeviceToHost) != cudaSuccess) return 7;
         bool mono = true;
         for (size_t c = 1; c < t.size(); ++c) mono = mono && t[c] >= t[c - 1];
@@ -87,6 +87,6 @@ int main(int argc, char** argv) {
                     back.empty() ? -1.0 : double(back[0].w));
     }
     std::printf("facade ok: particles=%zu boundary=%zu frames=%d calls=%zu n_sub=%zu device_pos=%p\n", n,
-                boundary.pos.size(), frames, calls, system.GetNumOfSubTimeSteps(), static_cast<void*>(dpos));
+                boundary.pos.size(), frames, calls, system.GetNumOfSubTimeSteps(), static_cast<const void*>(dpos));
     return dpos ? 0 : 6;
 }
