@@ -195,12 +195,13 @@ def reference_gpu_baseline(sc, calls=10):
             "path": "reference seepage_flows_cuda (-use_fast_math, sm_103a): CudaSFSystem::UpdateSystem(1/30 s)"}
 
 
-def batched_comparison(stream, substeps=100, n_scenes=64, blocks=2):
+def batched_comparison(stream, substeps=100, n_scenes=64, blocks=10):
     """The batched-ensemble workload: n_scenes independent scenes (log-uniform
     2k-60k particles, per-scene friction/capillary/permeability) advanced in
     the same launches by one handle, against a loop over one handle per scene
-    on the same GPU. Both replay captured graphs of `substeps`-substep blocks
-    (graph capture covers two substeps; a block is substeps/2 replays)."""
+    on the same GPU, for the ensemble's 1000 substeps (10 blocks of 100). Both
+    replay captured graphs of `substeps`-substep blocks (graph capture covers
+    two substeps; a block is substeps/2 replays)."""
     import torch
 
     from sph_seepage_flows_gb300 import capi, scenes

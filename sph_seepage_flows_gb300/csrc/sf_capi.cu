@@ -201,6 +201,7 @@ struct sf_handle {
     float2* vrec2 = nullptr;  // gather records, rewritten every substep
     float4* grec4 = nullptr;
     unsigned int *keys = nullptr, *cs = nullptr, *bcs = nullptr;
+    unsigned char* bnear = nullptr;  // per cell: a boundary particle within the 27 cells
     unsigned int* nbrCnt = nullptr;
     int* bnbrCnt = nullptr;
     int* cnbrCnt = nullptr;
@@ -285,6 +286,7 @@ struct sf_handle {
         b.listsW.cnbr = cnbr;
         b.listsW.cs = cs;
         b.listsW.bcs = bcs;
+        b.listsW.bnear = bnear;
         b.listsW.M = totalSlots;
         b.listsW.cap = nbrCap;
         b.lists.cnt = nbrCnt;
@@ -295,6 +297,7 @@ struct sf_handle {
         b.lists.cnbr = cnbr;
         b.lists.cs = cs;
         b.lists.bcs = bcs;
+        b.lists.bnear = bnear;
         b.lists.M = totalSlots;
         b.lists.cap = nbrCap;
         b.pos4 = pos[cur];
@@ -382,6 +385,7 @@ struct sf_handle {
         devFree(cnbr);
         devFree(cs);
         devFree(bcs);
+        devFree(bnear);
         devFree(sc.keysAlt);
         devFree(sc.vals);
         devFree(sc.valsAlt);
@@ -710,6 +714,7 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
     SF_ALLOC(h->sc.digitTotal, sizeof(unsigned) * size_t(maxRadix));
     SF_ALLOC(h->cs, sizeof(unsigned) * (size_t(h->totalCells) + 1));
     SF_ALLOC(h->bcs, sizeof(unsigned) * (size_t(h->totalCells) + 1));
+    SF_ALLOC(h->bnear, std::max<size_t>(1, size_t(h->totalCells)));
     SF_ALLOC(h->bpos, sizeof(float4) * std::max<size_t>(1, size_t(h->totalB)));
     SF_ALLOC(h->blabel, sizeof(int) * std::max<size_t>(1, size_t(h->totalB)));
     SF_ALLOC(h->dScenes, sizeof(SceneDev) * n_scenes);
@@ -732,6 +737,7 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
     std::vector<float4> hbpos(std::max(1, h->totalB), make_float4(0, 0, 0, 0));
     std::vector<int> hblabel(std::max(1, h->totalB), 0);
     std::vector<unsigned> hbcs(size_t(h->totalCells) + 1, 0);
+    std::vector<unsigned char> hbnear(std::max<size_t>(1, size_t(h->totalCells)), 0);
     std::vector<SceneState> hstate(n_scenes);
     for (int s = 0; s < n_scenes; ++s) {
         const sf_scene_init& in = inits[s];
@@ -766,6 +772,16 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
             hbcs[size_t(S.cell_off + c)] = run;
             run += cnt[c];
         }
+        // cells with a boundary particle in their 27-cell stencil: the density
+        // pass walks the boundary ranges only there
+        for (int c = 0; c < S.ncell; ++c) {
+            if (!cnt[c]) continue;
+            const int cx = c / (S.gy * S.gz), cy = (c / S.gz) % S.gy, cz = c % S.gz;
+            for (int x = std::max(cx - 1, 0); x <= std::min(cx + 1, S.gx - 1); ++x)
+                for (int y = std::max(cy - 1, 0); y <= std::min(cy + 1, S.gy - 1); ++y)
+                    for (int z = std::max(cz - 1, 0); z <= std::min(cz + 1, S.gz - 1); ++z)
+                        hbnear[size_t(S.cell_off + (x * S.gy + y) * S.gz + z)] = 1;
+        }
         for (int64_t i = 0; i < in.nb; ++i) {
             const int64_t o = order[i];
             hbpos[size_t(S.b_off + i)] = make_float4(in.bpos[3 * o], in.bpos[3 * o + 1], in.bpos[3 * o + 2], 0.f);
@@ -787,6 +803,7 @@ sf_status sf_create_batched(int32_t n_scenes, const sf_params* params, const sf_
         up(h->bpos, hbpos.data(), sizeof(float4) * hbpos.size(), "upload bpos") ||
         up(h->blabel, hblabel.data(), sizeof(int) * hblabel.size(), "upload blabel") ||
         up(h->bcs, hbcs.data(), sizeof(unsigned) * hbcs.size(), "upload bcs") ||
+        up(h->bnear, hbnear.data(), hbnear.size(), "upload bnear") ||
         up(h->dScenes, h->hScenes.data(), sizeof(SceneDev) * n_scenes, "upload scenes") ||
         up(h->dBlockScene, blockScene.data(), sizeof(int) * blockScene.size(), "upload blockScene") ||
         up(h->dState, hstate.data(), sizeof(SceneState) * n_scenes, "upload state"))
@@ -1740,7 +1757,8 @@ PassBuffers slabBuffers(const sf_handle* h, const AdjSlab& s) {
     b.lists.ccnt = s.ccnt;
     b.lists.cnbr = s.cnbr;
     b.lists.cs = s.cs;
-    b.listsW = NbrListsW{s.cnt, s.nbr, s.bcnt, s.bnbr, s.ccnt, s.cnbr, s.cs, h->bcs, b.lists.M, h->nbrCap};
+    b.listsW = NbrListsW{s.cnt, s.nbr, s.bcnt, s.bnbr, s.ccnt, s.cnbr, s.cs, h->bcs, h->bnear, b.lists.M,
+                         h->nbrCap};
     b.pos4 = s.pos;
     b.vel4 = s.vel;
     b.aux4 = s.aux;

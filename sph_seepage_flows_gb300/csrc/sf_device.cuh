@@ -138,9 +138,12 @@ __device__ __forceinline__ float3 spikyGrad(const SceneDev& S, float3 r) {
     float d = S.h - rlen;
     return S.spiky * d * d / rlen * r;
 }
-// AdhesionAkinci13::operator() (cuda_sph_kernel.cuh:196-202)
+// AdhesionAkinci13::operator() (cuda_sph_kernel.cuh:196-202). The fourth
+// root is taken as two IEEE square roots (within one ulp of x^(1/4), as close
+// as powf(x, 0.25f) and a fraction of its cost); the water adhesion it feeds
+// is checked against the reference arithmetic within a tolerance.
 __device__ __forceinline__ float adhesionSpline(const SceneDev& S, float r) {
-    if (2.f * r > S.h && r <= S.h) return S.adh_coef * powf(-4.f * r * r / S.h + 6.f * r - 2.f * S.h, 0.25f);
+    if (2.f * r > S.h && r <= S.h) return S.adh_coef * sqrtf(sqrtf(-4.f * r * r / S.h + 6.f * r - 2.f * S.h));
     return 0.f;
 }
 // QuadraticBezierCoeff::operator() (cuda_sf_utils.cuh:57-82)

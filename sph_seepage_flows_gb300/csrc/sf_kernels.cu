@@ -190,6 +190,8 @@ __global__ void __launch_bounds__(kSlotAlign, 6) kDensity(const SceneDev* __rest
     unsigned* __restrict__ bnb = L.bnbr + slot;
     int cS = 0, cW = 0, bc = 0;
     const int z0 = max(c.z - 1, 0), z1 = min(c.z + 1, S.gz - 1) + 1;
+    // no boundary particle within the 27 cells: the boundary ranges are empty
+    const bool nearB = !L.bnear || L.bnear[S.cell_off + localHash(S, c)] != 0;
 #pragma unroll 1
     for (int dx = -1; dx <= 1; ++dx) {
         const int x = c.x + dx;
@@ -226,6 +228,7 @@ __global__ void __launch_bounds__(kSlotAlign, 6) kDensity(const SceneDev* __rest
                     ++cW;
                 }
             }
+            if (!nearB) continue;
             const unsigned bEnd = L.bcs[base + z1];
             for (unsigned j = L.bcs[base + z0]; j < bEnd; ++j) {
                 if (!inReachFast(S, pi - xyz(bpos4[j]))) continue;
@@ -361,6 +364,9 @@ __global__ void __launch_bounds__(kSlotAlign) kDensityLanes(const SceneDev* __re
     };
     // the 9 column ranges of the stencil (particles and boundary), loaded
     // together up front: on a small scene the walk is a latency chain
+    // (the boundary ranges only where a boundary particle is within the 27
+    // cells; elsewhere they are empty)
+    const bool nearB = !L.bnear || L.bnear[S.cell_off + localHash(S, c)] != 0;
     unsigned cb[9], ce[9], bb[9], be[9];
 #pragma unroll
     for (int m = 0; m < 9; ++m) {
@@ -370,8 +376,10 @@ __global__ void __launch_bounds__(kSlotAlign) kDensityLanes(const SceneDev* __re
             const int base = S.cell_off + (x * S.gy + y) * S.gz;
             cb[m] = L.cs[base + z0];
             ce[m] = L.cs[base + z1];
-            bb[m] = L.bcs[base + z0];
-            be[m] = L.bcs[base + z1];
+            if (nearB) {
+                bb[m] = L.bcs[base + z0];
+                be[m] = L.bcs[base + z1];
+            }
         }
     }
     // chunk q of the stencil order: column m with pre[m] <= q < pre[m + 1]

@@ -48,6 +48,10 @@ struct NbrLists {
     const unsigned int* cnbr;
     const unsigned int* cs;   // particle cell table (total_cells + 1)
     const unsigned int* bcs;  // boundary cell table (total_cells + 1)
+    // per cell: 1 if a boundary particle lies in the cell or one of its 26
+    // neighbours (the boundary is static, so this is set once at creation);
+    // null means every cell walks its boundary ranges
+    const unsigned char* bnear;
     long long M;              // total slots
     int cap;                  // particle list capacity
 };
@@ -60,6 +64,7 @@ struct NbrListsW {
     unsigned int* cnbr;
     const unsigned int* cs;
     const unsigned int* bcs;
+    const unsigned char* bnear;
     long long M;
     int cap;
 };

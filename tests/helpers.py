@@ -64,7 +64,8 @@ def exact_fraction(a, b):
 
 
 # Outputs of each stage of the substep that the stage-by-stage comparisons
-# check, and the fields that pass through powf or reordered sums (compared
+# check, and the fields that pass through powf, the adhesion spline's fourth
+# root or reordered sums (compared
 # within tolerance; all others bit-for-bit).
 STAGE_OUTPUTS = {
     "sort": ["id", "label", "pos", "vel", "col", "mass", "radius", "cda0asat", "amcamcp", "max_saturation"],
