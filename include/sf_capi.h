@@ -31,6 +31,7 @@
  *   sf_adjoint_run       no reference counterpart (reverse-mode gradient of a trajectory loss)
  *   sf_set_adjoint_seed_scale  no reference counterpart (range of the adjoint's FP32 cotangents)
  *   sf_autotune          no reference counterpart (list capacity and block sizes of the passes)
+ *   sf_set_density_staging / sf_get_density_staging  no reference counterpart (shared-memory staging of the density pass's candidates)
  *   sf_get_list_capacity no reference counterpart (neighbour list capacity and its growth)
  *
  * Threading: handles are independent; one handle must not be used from two
@@ -317,6 +318,16 @@ sf_status sf_set_tuning(sf_handle* h, int32_t block_size, int32_t items_per_thre
  * at the next substep (captured graphs are dropped). */
 sf_status sf_set_lanes(sf_handle* h, int32_t lanes);
 
+/* Shared-memory staging of the density pass (no reference counterpart), for
+ * one thread per particle: 1 makes each block copy the stencil columns of its
+ * particles' one or two (x, y) cell columns into shared memory and test every
+ * candidate from there (blocks spanning more columns, or with more candidates
+ * than 14 per thread, walk global memory); 0 walks global memory. Lists and
+ * results are identical either way; sf_autotune times both. Takes effect at
+ * the next substep (captured graphs are dropped). */
+sf_status sf_set_density_staging(sf_handle* h, int32_t staged);
+sf_status sf_get_density_staging(const sf_handle* h, int32_t* staged);
+
 /* Autotuner (no reference counterpart). Sizes the neighbour lists for the
  * current state (list capacity = largest neighbour count + 25%, a multiple of
  * 32 in [64, 256]; sf_create does this once for the initial state), then
@@ -325,7 +336,8 @@ sf_status sf_set_lanes(sf_handle* h, int32_t lanes);
  * 1, 2, 4 and 8 threads per
  * particle, each neighbour pass with 64, 128 and 256 threads per block
  * (density, average flow, voidage/adhesion, sand momentum, water momentum;
- * the integrator keeps its size); it keeps the fastest sort tiles and the
+ * the integrator keeps its size; with one thread per particle the density
+ * pass with and without its shared-memory staging); it keeps the fastest sort tiles and the
  * lane count with the smallest sum of its passes' best times, with those
  * block sizes. The state is not advanced. block_sizes_out (6 entries, in
  * that pass order then the integrator) and list_capacity_out may be NULL;

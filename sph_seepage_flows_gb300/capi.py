@@ -84,6 +84,8 @@ def load(path: str = LIB_PATH):
         "sf_get_list_capacity": (i32, [H, P(i32), P(i64)]),
         "sf_set_tuning": (i32, [H, i32, i32]),
         "sf_set_lanes": (i32, [H, i32]),
+        "sf_set_density_staging": (i32, [H, i32]),
+        "sf_get_density_staging": (i32, [H, P(i32)]),
         "sf_get_tuning": (i32, [H, P(i32), P(i32), P(i32), P(i32)]),
         "sf_autotune": (i32, [H, f32, P(i32), P(i32)]),
         "sf_last_error_string": (ctypes.c_char_p, [H]),
@@ -332,7 +334,18 @@ class Simulation:
         lanes, items, digit = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
         self._check(self.lib.sf_get_tuning(self.h, None, ctypes.byref(lanes), ctypes.byref(items),
                                            ctypes.byref(digit)))
-        return {"lanes": lanes.value, "sort_items": items.value, "sort_digit_bits": digit.value}
+        return {"lanes": lanes.value, "sort_items": items.value, "sort_digit_bits": digit.value,
+                "density_staged": self.density_staging()}
+
+    def set_density_staging(self, staged: bool):
+        """sf_set_density_staging: the one-lane density pass tests its
+        candidates from a shared-memory copy of its block's stencil columns."""
+        self._check(self.lib.sf_set_density_staging(self.h, int(bool(staged))))
+
+    def density_staging(self) -> int:
+        v = ctypes.c_int32()
+        self._check(self.lib.sf_get_density_staging(self.h, ctypes.byref(v)))
+        return v.value
 
     # -------------------------------------------------------------- adjoint
     def adjoint(self, dt: float, n_substeps: int, target, checkpoint_every: int | None = None,

@@ -235,6 +235,7 @@ struct sf_handle {
     int64_t listGrowths = 0;
     int block[kTunedPasses] = {kSlotAlign, kSlotAlign, kSlotAlign, kSlotAlign, kSlotAlign, kSlotAlign};
     int lanes = 1;  // threads per slot of the momentum passes and the adjoint pair kernels
+    int densityStaged = 0;  // the one-lane density pass stages its candidates in shared memory (tuned)
     unsigned int* dProbe = nullptr;       // neighbour-count probe word
     // reverse-mode buffers, allocated by the first sf_adjoint_run
     AdjBuffers adj{};
@@ -274,6 +275,7 @@ struct sf_handle {
         c.slotBlocks = slotBlocks;
         for (int k = 0; k < kTunedPasses; ++k) c.block[k] = block[k];
         c.lanes = lanes;
+        c.densityStaged = densityStaged;
         return c;
     }
     PassBuffers buffers() const {
@@ -1553,6 +1555,20 @@ sf_status sf_set_tuning(sf_handle* h, int32_t block_size, int32_t items_per_thre
     return SF_OK;
 }
 
+sf_status sf_set_density_staging(sf_handle* h, int32_t staged) {
+    if (!h) return SF_ERR_INVALID;
+    if (staged != 0 && staged != 1) return h->fail(SF_ERR_INVALID, "staged must be 0 or 1");
+    h->densityStaged = staged;
+    h->dropGraphs();
+    return SF_OK;
+}
+
+sf_status sf_get_density_staging(const sf_handle* h, int32_t* staged) {
+    if (!h || !staged) return SF_ERR_INVALID;
+    *staged = h->densityStaged;
+    return SF_OK;
+}
+
 sf_status sf_set_lanes(sf_handle* h, int32_t lanes) {
     if (!h) return SF_ERR_INVALID;
     if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8)
@@ -1627,36 +1643,46 @@ sf_status sf_autotune(sf_handle* h, float dt, int32_t* block_sizes_out, int32_t*
     const int stages[kTunedPasses - 1] = {SF_STAGE_DENSITY, SF_STAGE_AVGFLOW, SF_STAGE_VOIDAGE_ADHESION,
                                           SF_STAGE_SAND_MOMENTUM, SF_STAGE_WATER_MOMENTUM};
     for (int s = SF_STAGE_DENSITY; s <= SF_STAGE_WATER_MOMENTUM && st == SF_OK; ++s) st = runStage(h, s, dt, 0);
+    // (with one lane the density pass is timed with and without its
+    // shared-memory staging as well)
     float bestTotal = 0.f;
-    int bestLanes = h->lanes, bestBlock[kTunedPasses - 1];
+    int bestLanes = h->lanes, bestBlock[kTunedPasses - 1], bestStaged = 0;
     for (int p = 0; p < kTunedPasses - 1; ++p) bestBlock[p] = h->block[p];
     for (int lanes : {1, 2, 4, 8}) {
         if (st) break;
         h->lanes = lanes;
         float total = 0.f;
-        int block[kTunedPasses - 1];
+        int block[kTunedPasses - 1], staged = 0;
         for (int p = 0; p < kTunedPasses - 1 && st == SF_OK; ++p) {
             float best = 0.f;
             block[p] = h->block[p];
-            for (int bs : candidates) {
-                h->block[p] = bs;
-                float ms = 0.f;
-                if ((st = timed([&] { return runStage(h, stages[p], dt, 0); }, ms))) break;
-                if (best == 0.f || ms < best) {
-                    best = ms;
-                    block[p] = bs;
+            const int forms = (p == kPassDensity && lanes == 1) ? 2 : 1;
+            for (int f = 0; f < forms && st == SF_OK; ++f) {
+                h->densityStaged = f;
+                for (int bs : candidates) {
+                    h->block[p] = bs;
+                    float ms = 0.f;
+                    if ((st = timed([&] { return runStage(h, stages[p], dt, 0); }, ms))) break;
+                    if (best == 0.f || ms < best) {
+                        best = ms;
+                        block[p] = bs;
+                        if (p == kPassDensity) staged = f;
+                    }
                 }
             }
+            h->densityStaged = 0;
             h->block[p] = block[p];
             total += best;
         }
         if (st == SF_OK && (bestTotal == 0.f || total < bestTotal)) {
             bestTotal = total;
             bestLanes = lanes;
+            bestStaged = staged;
             for (int p = 0; p < kTunedPasses - 1; ++p) bestBlock[p] = block[p];
         }
     }
     h->lanes = bestLanes;
+    h->densityStaged = bestStaged;
     for (int p = 0; p < kTunedPasses - 1; ++p) h->block[p] = bestBlock[p];
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -28,6 +28,8 @@
 // neighbours before water neighbours, instead of one sub-loop per term and
 // cell, which reorders their FP32 sums (differences ~1e-7 of the sum of term
 // magnitudes).
+#include <algorithm>
+
 #include "sf_device.cuh"
 #include "sf_kernels.h"
 #include "sf_neighbors.cuh"
@@ -160,6 +162,105 @@ __device__ __forceinline__ void recordListNeed(const NbrListsW& L, unsigned int&
     if ((threadIdx.x & 31u) == unsigned(__ffs(active) - 1)) atomicMax(&need, m);
 }
 
+// Shared-memory staging of a block's stencil candidates (kDensity<true>).
+// The slots of a block are consecutive in the cell order, so their particles
+// lie in one or two (x, y) cell columns for nearly every block; for each such
+// source column the block copies the 9 stencil columns over the z-cells its
+// particles reach into shared memory (coalesced, one warp per column) and the
+// walk reads every candidate from there. sG[k] / sO[k]: first slot and shared
+// offset of staged column k = 9 * source column + stencil column. A block with
+// more source columns, or with more candidates than its shared capacity,
+// walks global memory. Lists and results are identical either way; the tuner
+// times both forms.
+constexpr int kStageSources = 2;
+constexpr int kStageCols = 9 * kStageSources;
+constexpr int kBigInt = 0x7fffffff;
+struct StageTable {
+    unsigned g[kStageCols];      // first global slot of each staged column
+    unsigned o[kStageCols + 1];  // shared offset of each staged column (+ total)
+    int red[8];                  // block reductions (see stageBlock)
+};
+
+// Fills the table and the shared positions of the block's candidates;
+// returns the number of staged source columns (0: walk global memory). Every
+// thread of the block calls it.
+__device__ __forceinline__ int stageBlock(const SceneDev& S, const NbrListsW& L, const float4* __restrict__ pos4,
+                                          bool live, int3 c, StageTable& T, float4* sPos, int stageCap) {
+    const int lane = threadIdx.x & 31;
+    const int col = c.x * S.gy + c.y;
+    if (threadIdx.x < 8) T.red[threadIdx.x] = kBigInt;
+    __syncthreads();
+    {  // first and last source column (maxima as minima of negations)
+        const int a = __reduce_min_sync(~0u, live ? col : kBigInt);
+        const int b = __reduce_min_sync(~0u, live ? -col : kBigInt);
+        if (lane == 0) {
+            atomicMin(&T.red[0], a);
+            atomicMin(&T.red[1], b);
+        }
+    }
+    __syncthreads();
+    const int colA = T.red[0], colB = -T.red[1];
+    {  // any column between them, and the z-range of each
+        const bool inA = live && col == colA, inB = live && col == colB;
+        const int m = __reduce_min_sync(~0u, live && col > colA ? col : kBigInt);
+        const int za = __reduce_min_sync(~0u, inA ? c.z : kBigInt);
+        const int zA = __reduce_min_sync(~0u, inA ? -c.z : kBigInt);
+        const int zb = __reduce_min_sync(~0u, inB ? c.z : kBigInt);
+        const int zB = __reduce_min_sync(~0u, inB ? -c.z : kBigInt);
+        if (lane == 0) {
+            atomicMin(&T.red[2], m);
+            atomicMin(&T.red[3], za);
+            atomicMin(&T.red[4], zA);
+            atomicMin(&T.red[5], zb);
+            atomicMin(&T.red[6], zB);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        // lane k < 9 * sources: staged column k, its range from the cell table
+        const int nsrc = colA == kBigInt ? 0 : (colB == colA ? 1 : (T.red[2] == colB ? 2 : 3));
+        unsigned g = 0u, cnt = 0u;
+        const int src = lane / 9, m = lane % 9;
+        if (nsrc <= kStageSources && src < nsrc) {
+            const int cl = src ? colB : colA;
+            const int x = cl / S.gy + m / 3 - 1, y = cl % S.gy + m % 3 - 1;
+            const int zlo = max((src ? T.red[5] : T.red[3]) - 1, 0);
+            const int zhi = min(-(src ? T.red[6] : T.red[4]) + 1, S.gz - 1) + 1;
+            if (x >= 0 && x < S.gx && y >= 0 && y < S.gy) {
+                const int base = S.cell_off + (x * S.gy + y) * S.gz;
+                g = L.cs[base + zlo];
+                cnt = L.cs[base + zhi] - g;
+            }
+        }
+        unsigned inc = cnt;  // inclusive prefix of the column lengths
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned t = __shfl_up_sync(~0u, inc, o);
+            if (lane >= o) inc += t;
+        }
+        if (lane < kStageCols) {
+            T.g[lane] = g;
+            T.o[lane] = inc - cnt;
+        }
+        const unsigned total = __shfl_sync(~0u, inc, 31);
+        if (lane == 0) {
+            T.o[kStageCols] = total;
+            T.red[7] = (nsrc >= 1 && nsrc <= kStageSources && total <= unsigned(stageCap)) ? nsrc : 0;
+        }
+    }
+    __syncthreads();
+    const int staged = T.red[7];
+    if (staged) {
+        const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        for (int k = warp; k < 9 * staged; k += nw) {
+            const unsigned g = T.g[k], o = T.o[k], cnt = T.o[k + 1] - o;
+            for (unsigned i = lane; i < cnt; i += 32u) sPos[o + i] = pos4[g + i];
+        }
+        __syncthreads();
+    }
+    return staged;
+}
+
 // Builds the neighbour lists (sand / water / boundary, each in stencil
 // order, plus the sand-sand contact list) and computes the density, fused
 // with ComputeSFPressureByTait_CUDA (cuda_wcsph_sf_solver_gpu.cuh:19-44) or
@@ -171,16 +272,24 @@ __device__ __forceinline__ void recordListNeed(const NbrListsW& L, unsigned int&
 // over the finished lists, where the lanes of a warp stay together.
 // The walk is bound by load latency: a register budget of 40 (6 blocks of
 // kSlotAlign threads per SM) buys occupancy that outweighs the few values it
-// moves to the stack.
-__global__ void __launch_bounds__(kSlotAlign, 6) kDensity(const SceneDev* __restrict__ scenes,
-                                                       const int* __restrict__ blockScene,
-                                                       SceneState* __restrict__ state, NbrListsW L,
-                                                       const float4* __restrict__ pos4,
-                                                       const float4* __restrict__ bpos4, float4* __restrict__ vel4,
-                                                       float4* __restrict__ aux4) {
+// moves to the stack. kStaged reads the candidates from the block's staged
+// copy (stageBlock, stageCap positions of dynamic shared memory; 48
+// registers, since its shared memory already bounds the resident blocks).
+template <bool kStaged>
+__global__ void __launch_bounds__(kSlotAlign, kStaged ? 5 : 6) kDensity(const SceneDev* __restrict__ scenes,
+                                                                     const int* __restrict__ blockScene,
+                                                                     SceneState* __restrict__ state, NbrListsW L,
+                                                                     const float4* __restrict__ pos4,
+                                                                     const float4* __restrict__ bpos4,
+                                                                     float4* __restrict__ vel4,
+                                                                     float4* __restrict__ aux4, int stageCap) {
     SF_SLOT_PROLOGUE
+    extern __shared__ float4 sPos[];
+    __shared__ StageTable T;
     if (slot == S.slot_off) state[sid].amax_bits = 0u;
     const float4 pi4 = pos4[slot];
+    int staged = 0;
+    if constexpr (kStaged) staged = stageBlock(S, L, pos4, pi4.w != 0.f, cellOf(S, xyz(pi4)), T, sPos, stageCap);
     if (pi4.w == 0.f) return;
     const float3 pi = xyz(pi4);
     const int3 c = cellOf(S, pi);
@@ -190,6 +299,9 @@ __global__ void __launch_bounds__(kSlotAlign, 6) kDensity(const SceneDev* __rest
     unsigned* __restrict__ bnb = L.bnbr + slot;
     int cS = 0, cW = 0, bc = 0;
     const int z0 = max(c.z - 1, 0), z1 = min(c.z + 1, S.gz - 1) + 1;
+    // staged columns of this particle's source column
+    int src9 = 0;
+    if constexpr (kStaged) src9 = (staged == 2 && c.x * S.gy + c.y != T.red[0]) ? 9 : 0;
     // no boundary particle within the 27 cells: the boundary ranges are empty
     const bool nearB = !L.bnear || L.bnear[S.cell_off + localHash(S, c)] != 0;
 #pragma unroll 1
@@ -210,11 +322,22 @@ __global__ void __launch_bounds__(kSlotAlign, 6) kDensity(const SceneDev* __rest
             for (unsigned j0 = L.cs[base + z0]; j0 < jEnd; j0 += 32u) {
                 const int n = int(min(32u, jEnd - j0));
                 unsigned rev = 0u, srev = 0u;
+                if (kStaged && staged) {
+                    const int k = src9 + (dx + 1) * 3 + (dy + 1);
+                    const float4* sp = sPos + (int(j0) + int(T.o[k]) - int(T.g[k]));
 #pragma unroll 4
-                for (int t = 0; t < n; ++t) {
-                    const float4 q = pos4[j0 + unsigned(t)];
-                    rev = __funnelshift_l(__float_as_uint(reachSign(S, pi - xyz(q))), rev, 1);
-                    srev = __funnelshift_l(__float_as_uint(q.w), srev, 1);
+                    for (int t = 0; t < n; ++t) {
+                        const float4 q = sp[t];
+                        rev = __funnelshift_l(__float_as_uint(reachSign(S, pi - xyz(q))), rev, 1);
+                        srev = __funnelshift_l(__float_as_uint(q.w), srev, 1);
+                    }
+                } else {
+#pragma unroll 4
+                    for (int t = 0; t < n; ++t) {
+                        const float4 q = pos4[j0 + unsigned(t)];
+                        rev = __funnelshift_l(__float_as_uint(reachSign(S, pi - xyz(q))), rev, 1);
+                        srev = __funnelshift_l(__float_as_uint(q.w), srev, 1);
+                    }
                 }
                 const unsigned hit = __brev(rev) >> (32 - n), sand = __brev(srev) >> (32 - n);
                 // the list overflows when the two parts meet: from then on
@@ -856,9 +979,16 @@ void launchDensity(const LaunchCtx& c, const PassBuffers& b) {
     case 4: launchDensityLanes<4>(c, b); break;
     case 8: launchDensityLanes<8>(c, b); break;
     default:
-        kDensity<<<grid(c, kPassDensity), c.block[kPassDensity], 0, c.stream>>>(c.scenes, c.blockScene, c.state,
-                                                                                b.listsW, b.pos4, b.bpos4, b.vel4,
-                                                                                b.aux4);
+        if (c.densityStaged) {
+            // 14 positions per thread (a block of 128 consecutive slots
+            // needs ~10.4 on the 1M embankment), within 48 KB per block
+            const int cap = std::min(14 * c.block[kPassDensity], kDensityStageMax);
+            kDensity<true><<<grid(c, kPassDensity), c.block[kPassDensity], size_t(cap) * sizeof(float4), c.stream>>>(
+                c.scenes, c.blockScene, c.state, b.listsW, b.pos4, b.bpos4, b.vel4, b.aux4, cap);
+        } else {
+            kDensity<false><<<grid(c, kPassDensity), c.block[kPassDensity], 0, c.stream>>>(
+                c.scenes, c.blockScene, c.state, b.listsW, b.pos4, b.bpos4, b.vel4, b.aux4, 0);
+        }
         break;
     }
 }

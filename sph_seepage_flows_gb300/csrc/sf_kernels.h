@@ -23,7 +23,13 @@ struct LaunchCtx {
     int slotBlocks;           // total slots / kSlotAlign
     int block[kTunedPasses];  // threads per block of each tuned pass
     int lanes;                // threads per slot of the momentum passes (1, 2, 4 or 8)
+    int densityStaged;        // 1: the one-lane density pass stages its candidates in shared memory
 };
+
+// Largest shared staging of the density pass, in positions (16 B each): with
+// the pass's own shared table it stays within the 48 KB a block gets without
+// an opt-in.
+constexpr int kDensityStageMax = 3008;
 
 // Neighbour lists of the current substep (column-major: entry k of slot i at
 // k * M + i). Particle lists hold sand neighbours from entry 0 upwards and

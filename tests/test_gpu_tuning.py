@@ -3,7 +3,10 @@ every pass computes each slot's outputs independently of the block shape,
 so substeps run with any block size are bit-identical. The list capacity
 probe sizes the neighbour lists so dense scenes do not overflow them. The
 lane count (sf_set_lanes: threads per particle) leaves the lists and every
-field up to the momentum passes bit-identical; the momentum sums regroup."""
+field up to the momentum passes bit-identical; the momentum sums regroup.
+The density pass's shared-memory staging (sf_set_density_staging) changes
+where candidates are read from, not which or in what order: lists and
+substeps are bit-identical with and without it."""
 
 import numpy as np
 import pytest
@@ -38,6 +41,7 @@ def test_block_size_does_not_change_results(cuda_lib, name):
             assert np.array_equal(out[f], ref[f]), (bs, f)
     out, info = run(sc, lambda s, dt: s.autotune(dt))
     assert set(info["block_sizes"].values()) <= {64, 128, 256}
+    assert info["density_staged"] in (0, 1)
     assert info["lanes"] in (1, 2, 4, 8) and info["sort_items"] in (1, 2, 4, 8)
     assert 8 <= info["sort_digit_bits"] <= 11
     # the tuner's block sizes and sort tiles change nothing; its lane count
@@ -130,3 +134,48 @@ def test_set_lanes_rejects_bad_counts(cuda_lib):
     for bad in (3, 16, -1):
         with pytest.raises(SfError):
             sim.set_lanes(bad)
+
+
+def one_lane(staged, bs):
+    def tune(sim, dt):
+        sim.set_lanes(1)
+        sim.set_tuning(bs)
+        sim.set_density_staging(staged)
+        assert sim.density_staging() == int(staged)
+    return tune
+
+
+@pytest.mark.parametrize("name", ["tiny", "plain_small"])
+def test_density_staging_does_not_change_results(cuda_lib, name):
+    """Four substeps with the density candidates staged in shared memory, at
+    every block size, equal the unstaged run bit for bit (one thread per
+    particle, the path large scenes take)."""
+    sc = getattr(scenes, name)()
+    ref, _ = run(sc, one_lane(False, 128))
+    for bs in (32, 64, 128, 256):
+        out, _ = run(sc, one_lane(True, bs))
+        for f in FIELDS:
+            assert np.array_equal(out[f], ref[f]), (bs, f)
+
+
+def test_density_staging_identical_lists_at_full_size(cuda_lib):
+    """The 1M embankment, where nearly every block stages its candidates:
+    neighbour counts, density and pressure of the density stage are the same
+    bits with and without staging, at 128 and 256 threads per block (at 256
+    the denser blocks exceed the shared capacity and walk global memory)."""
+    from sph_seepage_flows_gb300.capi import Simulation
+    sc = scenes.plain_large()
+    dt = reference_dt(sc.params, sc.bparams, sc.sparams)[1]
+    outs = {}
+    for staged, bs in ((False, 128), (True, 128), (True, 256)):
+        sim = Simulation(sc)
+        one_lane(staged, bs)(sim, dt)
+        sim.stage("sort", dt)
+        sim.stage("density", dt)
+        outs[(staged, bs)] = {f: sim.field(f) for f in ("neighbors", "density", "pressure", "id")}
+        assert sim.check_error() == 0
+        sim.close()
+    ref = outs[(False, 128)]
+    for key in ((True, 128), (True, 256)):
+        for f in ref:
+            assert np.array_equal(outs[key][f], ref[f]), (key, f)
