@@ -59,19 +59,22 @@ STAGE_BYTES = {
 BYTES_PER_SUBSTEP = sum(STAGE_BYTES.values())  # 753
 
 # DRAM bytes (read + write) per launch of each stage's main kernel on the 1M
-# workload, from one ncu capture, tagged with the digest of the kernel sources
-# it was taken on (csrc_digest()). When the sources have changed since, the
-# figure no longer describes the running kernels and is reported as null.
-NCU_TRAFFIC_DIGEST = "972e6fd78a76"
-NCU_TRAFFIC = {"density": 284.8e6}
+# workload, from one ncu capture, tagged with the digest of the sources that
+# kernel is compiled from (its translation unit and the headers it includes,
+# csrc_digest(KERNEL_SOURCES[stage])) at the capture. When those sources have
+# changed since, the figure no longer describes the running kernel and is
+# reported as null.
+KERNEL_SOURCES = {"density": ("sf_kernels.cu", "sf_kernels.h", "sf_device.cuh", "sf_neighbors.cuh")}
+NCU_TRAFFIC = {"density": (284.8e6, "46927a8602d4")}
 
 
-def csrc_digest() -> str:
-    """sha256 (first 12 hex digits) of the CUDA sources, in name order."""
+def csrc_digest(names=None) -> str:
+    """sha256 (first 12 hex digits) of the named CUDA sources (default: all),
+    in name order."""
     import hashlib
     d = hashlib.sha256()
     csrc = os.path.join(ROOT, "sph_seepage_flows_gb300", "csrc")
-    for name in sorted(os.listdir(csrc)):
+    for name in sorted(names or os.listdir(csrc)):
         if name.endswith((".cu", ".cuh", ".h")):
             with open(os.path.join(csrc, name), "rb") as f:
                 d.update(name.encode() + b"\0" + f.read())
@@ -466,11 +469,11 @@ def run_ours(args, rank, world):
             stage_ms[s] += evs[k].elapsed_time(evs[k + 1]) / reps
     top = max(stage_ms, key=stage_ms.get)
     peak, peak_kind = peaks()
-    digest = csrc_digest()
+    digest = csrc_digest(KERNEL_SOURCES.get(top))
     traffic, traffic_source = None, "no ncu capture of the current kernel sources"
-    if args.workload == "plain_large" and digest == NCU_TRAFFIC_DIGEST and top in NCU_TRAFFIC:
-        traffic = NCU_TRAFFIC[top]
-        traffic_source = f"ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, sources {digest}"
+    if args.workload == "plain_large" and top in NCU_TRAFFIC and digest == NCU_TRAFFIC[top][1]:
+        traffic = NCU_TRAFFIC[top][0]
+        traffic_source = f"ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, kernel sources {digest}"
     achieved = STAGE_BYTES[top] * n / (stage_ms[top] * 1e-3) / 1e9
 
     # e2e through the C ABI with pinned host buffers

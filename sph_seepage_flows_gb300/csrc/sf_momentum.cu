@@ -140,13 +140,17 @@ __global__ void __launch_bounds__(kSlotAlign, 5) kWaterMomentum(
         forWaterNeighbors<G, true>(S, L, slot, pi, pos4, [&](int j) {
             if (j == slot) return;
             const float4 pj = pos4[j];
-            const float3 dij = pi - xyz(pj);
             const float4 gj = grec4[j];  // (velocity, P)
+            // D of the neighbour, loaded with its position and record for
+            // every pair (only approaching pairs use it): its latency then
+            // overlaps the pressure term instead of stalling inside the
+            // viscosity branch
+            const float dj = dp[j].x;
+            const float3 dij = pi - xyz(pj);
             const float3 nab = spikyGrad(S, dij);
             a += -pj.w * (pterm_i + gj.w) * nab;
             const float dd = dot3(vi - xyz(gj), dij);
             if (dd < 0.f) {
-                const float dj = dp[j].x;
                 const float pij = -S.nu / (di + dj) * (dd / (dot3(dij, dij) + kEps));
                 a += -pj.w * pij * nab;
             }
