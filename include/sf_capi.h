@@ -27,6 +27,7 @@
  *   sf_add_sph_particles CudaSFParticles::AddSphParticles (src/kiri_pbs_cuda/particle/cuda_sf_particles.cu:50-68)
  *   sf_run_stage         the protected per-pass methods of CudaSphSFSolver (src/kiri_pbs_cuda/solver/seepage_flow/cuda_sph_sf_solver.cu:20-402)
  *   sf_substeps_fixed    fixed-substep mode of main.cpp:250-258 (no reference counterpart for the graph capture)
+ *   sf_reset_order       no reference counterpart (creation order back, for repeatable runs from a reset state)
  *   sf_create_batched    no reference counterpart (independent scenes in one launch)
  *   sf_adjoint_run       no reference counterpart (reverse-mode gradient of a trajectory loss)
  *   sf_set_adjoint_seed_scale  no reference counterpart (range of the adjoint's FP32 cotangents)
@@ -220,6 +221,15 @@ sf_status sf_step(sf_handle* h, float render_interval, int64_t* n_substeps_out, 
  * (the GPU keeps the newer block queued), so that the neighbour lists can grow
  * within the call (see sf_get_list_capacity). */
 sf_status sf_substeps_fixed(sf_handle* h, float dt, int64_t n);
+
+/* Puts every scene's particles back in creation order (slot = particle id),
+ * no reference counterpart. The sort of the next substep is stable, so its
+ * order among the particles of a cell (and with it the FP32 order of every
+ * neighbour sum) follows the order before it: a state reset by particle id
+ * (sf_set_field with SF_ORDER_ID) after this call repeats a fresh handle's
+ * run bit for bit, where without it the previous run's order would carry
+ * over. The cell tables are invalid until the next substep. */
+sf_status sf_reset_order(sf_handle* h);
 
 /* One frame of the reference adaptive loop: while remaining > 1e-6:
  * sf_step(remaining); remaining -= remaining / N_sub. Single-scene handles only. */

@@ -51,6 +51,9 @@ def apply_theta(sim, s, base, theta):
 
 
 def reset_state(sim, s, base):
+    """Scene s back to its initial positions and velocities. Call
+    sim.reset_order() first so that the run repeats a fresh handle's (the
+    sort breaks ties within a cell by the order it finds)."""
     sim.set_field("pos", base.pos, order="id", scene=s)
     sim.set_field("vel", base.vel, order="id", scene=s)
 
@@ -121,6 +124,7 @@ def calibrate(scenes, targets, theta0, dt, n_substeps, checkpoint_every, iterati
     history = {"loss": [], "theta": [], "ms": [], "seed_scale": []}
     scales = np.full(len(scenes), INITIAL_SEED_SCALE)
     for it in range(iterations):
+        sim.reset_order()
         for s, sc in enumerate(scenes):
             reset_state(sim, s, sc)
             apply_theta(sim, s, sc, theta[s])

@@ -66,6 +66,7 @@ def load(path: str = LIB_PATH):
         "sf_get_params": (i32, [H, i32, P(SfParams)]),
         "sf_step": (i32, [H, f32, P(i64), P(f32)]),
         "sf_substeps_fixed": (i32, [H, f32, i64]),
+        "sf_reset_order": (i32, [H]),
         "sf_frame_adaptive": (i32, [H, f32, P(i64)]),
         "sf_run_stage": (i32, [H, i32, f32, i32]),
         "sf_get_field": (i32, [H, i32, i32, i32, ctypes.c_void_p, i64, i32]),
@@ -219,6 +220,11 @@ class Simulation:
 
     def substeps_fixed(self, dt: float, n: int):
         self._check(self.lib.sf_substeps_fixed(self.h, float(dt), int(n)))
+
+    def reset_order(self):
+        """sf_reset_order: every scene's particles back in creation order, so
+        that a state reset by id repeats a fresh handle's run bit for bit."""
+        self._check(self.lib.sf_reset_order(self.h))
 
     def frame_adaptive(self, render_interval: float) -> int:
         calls = ctypes.c_int64()

@@ -1514,6 +1514,47 @@ sf_status sf_add_sph_particles(sf_handle* h, int32_t scene, const float* pos3, i
     return SF_OK;
 }
 
+namespace {
+
+// Scatters one scene's persistent arrays from buffer set o to t by particle
+// id: live slot s goes to slotOff + pid[s]; parked slots keep their place.
+__global__ void kResetOrder(int slots, int n, int slotOff, const float4* __restrict__ pos, const float4* __restrict__ vel,
+                            const float4* __restrict__ col, const float4* __restrict__ mat,
+                            const float2* __restrict__ amc, const int* __restrict__ pid, float4* __restrict__ pos2,
+                            float4* __restrict__ vel2, float4* __restrict__ col2, float4* __restrict__ mat2,
+                            float2* __restrict__ amc2, int* __restrict__ pid2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= slots) return;
+    const int s = slotOff + i;
+    const int id = pid[s];
+    const int d = (i < n && id >= 0 && id < n) ? slotOff + id : s;
+    pos2[d] = pos[s];
+    vel2[d] = vel[s];
+    col2[d] = col[s];
+    mat2[d] = mat[s];
+    amc2[d] = amc[s];
+    pid2[d] = id;
+}
+
+}  // namespace
+
+sf_status sf_reset_order(sf_handle* h) {
+    if (!h) return SF_ERR_INVALID;
+    const int o = h->cur, t = 1 - h->cur;
+    for (int sc = 0; sc < h->nScenes; ++sc) {
+        const SceneDev& S = h->hScenes[sc];
+        const int slots = S.slot_cap;
+        if (slots <= 0) continue;
+        kResetOrder<<<(slots + 255) / 256, 256, 0, h->stream>>>(
+            slots, int(h->n[sc]), S.slot_off, h->pos[o], h->vel[o], h->col[o], h->mat[o], h->amc[o], h->pid[o],
+            h->pos[t], h->vel[t], h->col[t], h->mat[t], h->amc[t], h->pid[t]);
+        h->launches += 1;
+    }
+    h->cur = t;
+    h->sorted = false;
+    return h->cuda(cudaGetLastError(), "reset order launch");
+}
+
 sf_status sf_check_error(sf_handle* h, uint32_t* flags) {
     if (!h || !flags) return SF_ERR_INVALID;
     unsigned v = 0;

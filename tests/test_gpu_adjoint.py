@@ -204,3 +204,28 @@ def test_seed_scale_changes_no_gradient_bit(cuda_lib):
         with pytest.raises(SfError):
             sim.set_adjoint_seed_scale(bad)
     sim.close()
+
+
+def test_reset_order_repeats_a_fresh_run(cuda_lib):
+    """sf_reset_order puts the particles back in creation order: a gradient
+    run from positions and velocities reset by id then repeats a fresh
+    handle's run bit for bit (the first sort breaks ties within a cell by
+    the order it finds, and that order sets the FP32 order of every sum)."""
+    from sph_seepage_flows_gb300 import calibrate, scenes
+    from sph_seepage_flows_gb300.params import reference_dt
+    sc = scenes.tiny(seed=7)
+    dt = reference_dt(sc.params, sc.bparams, sc.sparams)[1]
+    target = calibrate.forward_targets([sc], [np.array([sc.params.dem_tan_friction_angle, 1.1, 1.1])], dt, 16)[0]
+    fresh = sim_of(sc)
+    ref = fresh.adjoint(dt, 16, target, checkpoint_every=8)
+    fresh.close()
+    sim = sim_of(sc)
+    sim.substeps_fixed(dt, 40)  # the particles move and the order changes
+    assert not np.array_equal(sim.field("id"), np.arange(sc.n, dtype=np.int32))
+    sim.reset_order()
+    assert np.array_equal(sim.field("id"), np.arange(sc.n, dtype=np.int32))
+    calibrate.reset_state(sim, 0, sc)
+    r = sim.adjoint(dt, 16, target, checkpoint_every=8)
+    for key in ("loss", "grad_params", "grad_pos0", "grad_vel0"):
+        assert np.array_equal(r[key], ref[key]), key
+    sim.close()
