@@ -22,8 +22,9 @@
 // Summation order. Every accumulator of the density, average-flow, voidage,
 // saturation and adhesion passes receives one label class of neighbours, in
 // stencil order, exactly as in the reference kernel, so those fields are
-// bit-identical to the reference's FP32 arithmetic (density near walls is
-// recomputed with the reference's fluid/boundary interleaving per cell). The
+// bit-identical to the reference's FP32 arithmetic (near walls the water
+// density merges its water and boundary lists cell by cell, the reference's
+// interleaving of fluid and boundary terms). The
 // two momentum passes evaluate all terms of a neighbour together, sand
 // neighbours before water neighbours, instead of one sub-loop per term and
 // cell, which reorders their FP32 sums (differences ~1e-7 of the sum of term
