@@ -68,6 +68,18 @@ KERNEL_SOURCES = {"density": ("sf_kernels.cu", "sf_kernels.h", "sf_device.cuh", 
 NCU_TRAFFIC = {"density": (282.0e6, "0abe114f76e1")}
 
 
+def roofline_traffic(stage: str, workload: str):
+    """(DRAM bytes per launch, where they come from) of the stage's kernel on
+    the 1M workload, or (None, why) when no capture describes its current
+    sources."""
+    if workload != "plain_large" or stage not in NCU_TRAFFIC:
+        return None, "no ncu capture of this kernel on this workload"
+    digest = csrc_digest(KERNEL_SOURCES.get(stage))
+    if digest != NCU_TRAFFIC[stage][1]:
+        return None, "no ncu capture of the current kernel sources"
+    return NCU_TRAFFIC[stage][0], f"ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, kernel sources {digest}"
+
+
 def csrc_digest(names=None) -> str:
     """sha256 (first 12 hex digits) of the named CUDA sources (default: all),
     in name order."""
@@ -470,11 +482,7 @@ def run_ours(args, rank, world):
             stage_ms[s] += evs[k].elapsed_time(evs[k + 1]) / reps
     top = max(stage_ms, key=stage_ms.get)
     peak, peak_kind = peaks()
-    digest = csrc_digest(KERNEL_SOURCES.get(top))
-    traffic, traffic_source = None, "no ncu capture of the current kernel sources"
-    if args.workload == "plain_large" and top in NCU_TRAFFIC and digest == NCU_TRAFFIC[top][1]:
-        traffic = NCU_TRAFFIC[top][0]
-        traffic_source = f"ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, kernel sources {digest}"
+    traffic, traffic_source = roofline_traffic(top, args.workload)
     achieved = STAGE_BYTES[top] * n / (stage_ms[top] * 1e-3) / 1e9
 
     # e2e through the C ABI with pinned host buffers
