@@ -229,3 +229,28 @@ def test_reset_order_repeats_a_fresh_run(cuda_lib):
     for key in ("loss", "grad_params", "grad_pos0", "grad_vel0"):
         assert np.array_equal(r[key], ref[key]), key
     sim.close()
+
+
+def test_reset_order_in_a_batched_handle(cuda_lib):
+    """sf_reset_order in a handle of several scenes: each scene's particles go
+    back to creation order within its own slots, and substeps from a state
+    reset by id equal a fresh handle's bit for bit."""
+    from sph_seepage_flows_gb300 import calibrate, scenes
+    from sph_seepage_flows_gb300.capi import Simulation
+    from sph_seepage_flows_gb300.params import reference_dt
+    sc = [scenes.tiny(seed=3), scenes.tiny(seed=4, sand=(6, 6, 6), water=(4, 4, 4))]
+    dt = reference_dt(sc[0].params, sc[0].bparams, sc[0].sparams)[1]
+    fresh = Simulation(sc)
+    fresh.substeps_fixed(dt, 10)
+    sim = Simulation(sc)
+    sim.substeps_fixed(dt, 30)
+    sim.reset_order()
+    for k, s in enumerate(sc):
+        assert np.array_equal(sim.field("id", scene=k), np.arange(s.n, dtype=np.int32)), k
+        calibrate.reset_state(sim, k, s)
+    sim.substeps_fixed(dt, 10)
+    for k in range(len(sc)):
+        for name in ("pos", "vel", "density", "id"):
+            assert np.array_equal(sim.field(name, scene=k), fresh.field(name, scene=k)), (k, name)
+    sim.close()
+    fresh.close()
