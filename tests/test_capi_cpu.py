@@ -60,3 +60,20 @@ def test_create_without_device_reports_no_device(lib):
     with pytest.raises(capi.SfError) as e:
         capi.Simulation(scenes.tiny())
     assert e.value.status == 5
+
+
+def test_header_is_plain_c(tmp_path):
+    """include/sf_capi.h is a C interface: it compiles as strict C99 and as
+    C++17 with no warnings."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no gcc")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "use.c"
+    src.write_text('#include "sf_capi.h"\nint main(void) { return SF_CAPI_VERSION > 0 ? 0 : 1; }\n')
+    for cmd in ([gcc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only"],
+                [shutil.which("g++") or "g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-x", "c++"]):
+        r = subprocess.run(cmd + ["-I", os.path.join(root, "include"), str(src)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
