@@ -199,10 +199,13 @@ def reference_gpu_baseline(sc, calls=10):
             return {"unavailable": "reference CUDA sources not staged (oracle/build_ref_cuda.sh)"}
     except Exception as e:  # noqa: BLE001 - a baseline leg reports, never aborts the bench
         return {"unavailable": f"reference CUDA build failed: {e}"[:300]}
+    import torch
     r = oracle.RefGpu(sc)
     T = 1.0 / 30.0
     r.update(T)
+    torch.cuda.nvtx.range_push("reference_gpu")  # lets a profiler capture exactly the timed calls
     ms = r.run(T, calls)
+    torch.cuda.nvtx.range_pop()
     nsub = r.num_substeps
     del r
     return {"value": sc.n * calls / (ms * 1e-3), "unit": "particle-substeps/s", "ms_per_substep": ms / calls,
