@@ -216,8 +216,8 @@ sf_status sf_get_params(const sf_handle* h, int32_t scene, sf_params* params);
 sf_status sf_step(sf_handle* h, float render_interval, int64_t* n_substeps_out, float* ms_out);
 
 /* n substeps of every scene at a fixed dt, replayed from captured CUDA graphs.
- * Calls of up to 256 substeps return without waiting for the GPU. Longer calls
- * wait, after each block of 256 substeps, until the block before it has run
+ * Calls of up to 64 substeps return without waiting for the GPU. Longer calls
+ * wait, after each block of 64 substeps, until the block before it has run
  * (the GPU keeps the newer block queued), so that the neighbour lists can grow
  * within the call (see sf_get_list_capacity). */
 sf_status sf_substeps_fixed(sf_handle* h, float dt, int64_t n);

@@ -1015,7 +1015,7 @@ sf_status queueSubstepsFixed(sf_handle* h, float dt, int64_t n) {
 }
 
 // Substeps between list checks in a long call.
-constexpr int64_t kListCheckEvery = 256;
+constexpr int64_t kListCheckEvery = 64;
 
 }  // namespace
 

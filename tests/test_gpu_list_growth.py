@@ -72,7 +72,7 @@ def test_lists_grow_at_the_next_call(cuda_lib):
 
 
 def test_lists_grow_within_a_long_call(cuda_lib):
-    """A call of more than 256 substeps waits, after each block of 256, for
+    """A call of more than 64 substeps waits, after each block of 64, for
     the block before it, and grows the lists there: the capacity has grown
     when the call returns."""
     a, b, cap0, dt = pair()
