@@ -254,3 +254,30 @@ def test_reset_order_in_a_batched_handle(cuda_lib):
             assert np.array_equal(sim.field(name, scene=k), fresh.field(name, scene=k)), (k, name)
     sim.close()
     fresh.close()
+
+
+def test_reset_order_after_added_particles(cuda_lib):
+    """Particles added by sf_add_sph_particles take the next ids; after some
+    substeps the order reset puts every particle, the added ones included,
+    at the slot of its id, with its position and velocity."""
+    from sph_seepage_flows_gb300 import scenes
+    from sph_seepage_flows_gb300.capi import Simulation
+    from sph_seepage_flows_gb300.params import reference_dt
+    sc = scenes.tiny(seed=5)
+    dt = reference_dt(sc.params, sc.bparams, sc.sparams)[1]
+    sim = Simulation(sc, capacity=sc.n + 64)
+    sim.substeps_fixed(dt, 4)
+    pts = np.array([[0.2, 0.34, 0.2], [0.22, 0.34, 0.2], [0.2, 0.34, 0.22]], np.float32)  # above the material
+    sim.add_sph_particles(pts, np.array([0.3, 0.6, 1.0], np.float32), np.array([0.0, -1.0, 0.0], np.float32),
+                          sc.params.sph_mass, sc.params.sph_particle_radius)
+    sim.substeps_fixed(dt, 20)
+    n = sim.size()
+    assert n == sc.n + 3
+    pos_by_id, vel_by_id = sim.field("pos", order="id"), sim.field("vel", order="id")
+    sim.reset_order()
+    assert np.array_equal(sim.field("id"), np.arange(n, dtype=np.int32))
+    assert np.array_equal(sim.field("pos"), pos_by_id)
+    assert np.array_equal(sim.field("vel"), vel_by_id)
+    sim.substeps_fixed(dt, 2)
+    assert sim.check_error() == 0
+    sim.close()
